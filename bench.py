@@ -1,0 +1,319 @@
+"""Throughput benchmark of the phase-retrieval iteration engine.
+
+Workload (one GPU): 512 x 512 complex64, population 64, RAAR with beta 0.87,
+random convex polygon object (6-12 vertices, ~120 px), 1e7 photons with
+Poisson noise, masked central disc of radius 8 plus two 4-px gap stripes.
+One step = one RAAR call of ``--iters`` iterations (default 100, one
+generation's worth) on the whole population: the reference's
+``Solver.RAAR(population, 100, 0.87)``.
+
+metric: iterations x individuals per second.  ``value`` is measured with the
+population resident in HBM; ``e2e`` goes through the C ABI with host buffers
+(pinned), copying the population in and the result out every step.
+Inputs (density 128 MiB + support 64 MiB + scratch 128 MiB) exceed the
+129 MB L2 between steps.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 512
+POP = 64
+BETA = 0.87
+B_PER_PIXEL_ITER = 24  # rho read+write 16 B, amplitude 4 B, support 4 B
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--iters", type=int, default=100)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--cpu-sample-s", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload(seed=1):
+    from s_spi_spring_gb300 import _lib, synthetic
+    I, _, _ = synthetic.polygon_pattern(seed=seed, n=N, diameter=120.0, photons=1e7, stop_radius=8, gap=4, stripes=2)
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    dens, S = synthetic.start_population(N, POP, 70.0, seed=seed + 1)
+    return A, dens, S
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(sample_s: float, threads: int | None = None):
+    """The CPU restatement of the path timed on the host cores (bounded sample
+    of the same workload: a few individuals, a few RAAR iterations)."""
+    from oracle import cpu_port
+    A, dens, S = workload()
+    return cpu_port.time_raar(A, dens, S, BETA, sample_s, threads=threads)
+
+
+def run_engine(args):
+    import torch
+    from s_spi_spring_gb300 import _lib
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    A, dens, S = workload()
+    eng = _lib.Engine(N, local)
+    eng.set_amplitudes(A)
+    eng.reserve(POP)
+    stream = torch.cuda.Stream(device=local)
+    eng.set_stream(stream.cuda_stream)
+    eng.upload(0, dens, S)
+    eng.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- device-resident throughput
+    for _ in range(args.warmup):
+        eng.raar(0, POP, args.iters, BETA, 0.0)
+    eng.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            eng.raar(0, POP, args.iters, BETA, 0.0)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    units_per_step = POP * args.iters
+    value = units_per_step * world / (ms_step / 1e3)
+
+    # ---- per-iteration time of the fused iteration kernels (row + column pass):
+    # a call of k iterations minus a call of 0 iterations, on the same stream
+    def timed_call(iters, reps=3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            eng.raar(0, POP, iters, BETA, 0.0)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_k = timed_call(args.iters)
+    t_0 = timed_call(0, reps=10)
+    t_iter_ms = (t_k - t_0) / args.iters
+    alg_bytes = B_PER_PIXEL_ITER * N * N * POP
+    achieved = alg_bytes / (t_iter_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+
+    # ---- end to end through the C ABI with pinned host buffers
+    h_dens = torch.empty((POP, N, N, 2), dtype=torch.float32, pin_memory=True)
+    h_supp = torch.empty((POP, N, N), dtype=torch.int32, pin_memory=True)
+    h_out = torch.empty((POP, N, N, 2), dtype=torch.float32, pin_memory=True)
+    h_dens.numpy()[...] = dens.view(np.float32).reshape(POP, N, N, 2)
+    h_supp.numpy()[...] = S
+    lib = _lib.load()
+    fp = lambda t: _lib.C.cast(t.data_ptr(), _lib.C.POINTER(_lib.C.c_float))
+    ip = lambda t: _lib.C.cast(t.data_ptr(), _lib.C.POINTER(_lib.C.c_int32))
+
+    def e2e_step():
+        _lib.call("spe_upload", eng.h, 0, POP, fp(h_dens), ip(h_supp))
+        _lib.call("spe_raar", eng.h, 0, POP, args.iters, BETA, 0.0)
+        _lib.call("spe_download", eng.h, 0, POP, fp(h_out), None)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    e1.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_value = units_per_step * world / (e2e_ms / 1e3)
+
+    out = {
+        "metric": "iter*individuals/s (RAAR, 512^2, population 64)",
+        "value": round(value, 1),
+        "unit": "iter*individuals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex64/f32",
+        "data": "synthetic (seeded polygon object, Poisson 1e7 photons, beamstop + 2 gap stripes)",
+        "config": {"workload": "memetic population RAAR: 512x512 complex64, population 64, beta 0.87, "
+                               f"{args.iters} iterations per step",
+                   "pattern": N, "population": POP, "iterations_per_step": args.iters,
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (320 MiB working set)"},
+        "e2e": {"value": round(e2e_value, 1), "unit": "iter*individuals/s",
+                "h2d_bytes_per_step": int(h_dens.numel() * 4 + h_supp.numel() * 4),
+                "d2h_bytes_per_step": int(h_out.numel() * 4)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "fused iteration (column pass + row pass), per iteration",
+                     "alg_bytes_per_launch": alg_bytes, "ms_per_iteration": round(t_iter_ms, 5),
+                     "peak_source": peak_kind},
+        "gpu_launches": args.steps * (2 * args.iters + 3),
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_baseline(args.cpu_sample_s)
+        except Exception as ex:  # the baseline must not hide the engine's line
+            out["cpu_baseline"] = {"error": str(ex)[:200]}
+    eng.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import cpu_port
+    A, dens, S = workload()
+    per = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_port.time_raar(A, dens, S, BETA, sample_s=max(2.0, args.cpu_sample_s / max(1, args.steps)),
+                                  threads=None)
+        if i >= args.warmup:
+            per.append(info["value"])
+    value = statistics.median(per)
+    out = {
+        "impl": "reference",
+        "metric": "iter*individuals/s (RAAR, 512^2, population 64)",
+        "value": round(value, 2),
+        "unit": "iter*individuals/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(POP * args.iters / value * 1e3, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "complex64/f32",
+        "data": "synthetic (seeded polygon object, Poisson 1e7 photons, beamstop + 2 gap stripes)",
+        "config": {"workload": "memetic population RAAR: 512x512 complex64, population 64, beta 0.87, "
+                               f"{args.iters} iterations per step",
+                   "pattern": N, "population": POP, "iterations_per_step": args.iters},
+        "cpu_baseline": {**info, "value": round(value, 2)},
+        "e2e": {"value": round(value, 2), "unit": "iter*individuals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,158 @@
+/*
+ * spe_engine.h -- C ABI of the GB300 phase-retrieval engine (SPRING
+ * HIO / RAAR / ER iteration, shrink-wrap, error metrics, alignment,
+ * population averages and memetic crossover).
+ *
+ * The engine replaces the reference's per-individual GPU context
+ * (MasterSPP/S_SPI_SPRING src/gpu/gpu_context.{h,cu} implementing the
+ * virtual interface of src/context.h:11-70) with a population-level seam:
+ * a whole population of N x N reconstructions lives in device memory and
+ * every call processes a contiguous range [first, first+count) of it in
+ * batched kernels.  The reference's Solver loops (src/solver.cpp:360-558,
+ * "#pragma omp parallel for" over individuals, one context per thread)
+ * become one call each.
+ *
+ * Conventions
+ *   - All arrays are row-major N x N, x fastest (index x + y*N), as the
+ *     reference's Reconstruction (src/reconstruction.h:99-100).
+ *   - density: interleaved complex64 (re, im) = std::complex<float> /
+ *     cufftComplex (src/datatypes.h:5-8); support: int32 (SUPPORTTYPE,
+ *     src/datatypes.h:11).
+ *   - Host pointers are copied, never aliased.  The engine owns its device
+ *     memory, stream and scratch.
+ *   - Every call returns SPE_OK (0) or an error code; spe_last_error()
+ *     gives the message of the calling thread's last failure.  (The
+ *     reference ignores CUDA status codes and prints cuFFT failures,
+ *     gpu_context.cu:750-752.)
+ *   - A handle is not thread safe; calls on one handle are serialised on
+ *     its stream.  Calls that return results to the host synchronise.
+ */
+#ifndef SPE_ENGINE_H
+#define SPE_ENGINE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  SPE_OK = 0,
+  SPE_ERR_INVALID = 1,     /* bad argument (size, range, null pointer)   */
+  SPE_ERR_CUDA = 2,        /* a CUDA runtime call or a launch failed      */
+  SPE_ERR_NOMEM = 3,       /* device or pinned allocation failed          */
+  SPE_ERR_UNSUPPORTED = 4, /* pattern size without a compiled FFT plan    */
+  SPE_ERR_STATE = 5        /* call out of order (no amplitudes, capacity)  */
+};
+
+/* One step of an algorithm sequence, as produced by the reference's
+ * Solver::get_algorithm (src/solver.cpp:84-159) from the op list of
+ * spring/alg_manager.py:105-143. */
+enum { SPE_OP_HIO = 0, SPE_OP_RAAR = 1, SPE_OP_ER = 2, SPE_OP_SW = 3, SPE_OP_SWA = 4 };
+typedef struct spe_op {
+  int32_t kind;       /* SPE_OP_*                                       */
+  int32_t iterations; /* HIO / RAAR / ER                                */
+  float beta;         /* HIO / RAAR                                     */
+  float sigma;        /* SW / SWA                                       */
+  float threshold;    /* SW                                             */
+  int32_t pixels;     /* SWA                                            */
+} spe_op;
+
+/* Per-individual results of Solver::Evaluate / Sequence, the fields of the
+ * reference's Reconstruction (src/reconstruction.h:101-110). */
+typedef struct spe_metrics {
+  float error;         /* error_fourier * (1 + realpen * reality)       */
+  float error_fourier; /* R-factor sqrt(sum (A-|F|)^2 / sum A^2)         */
+  float error_real;
+  float reality;       /* 1 - complexsum / modulesum                    */
+  float modulesum;
+  float complexsum;
+  float symmetry;
+} spe_metrics;
+
+typedef struct spe_engine spe_engine;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* spe_last_error(void);
+
+/* ABI version (major * 100 + minor). */
+int spe_version(void);
+
+/* Host-side pattern encoding of the reference's Solver constructor:
+ * Solver::set_boundaries (src/solver.cpp:209-289) then Solver::prepare
+ * (src/solver.cpp:173-206).  intensities: n x n float (masked = -1,
+ * saturated = -2 as spring/pattern_manager.py:77-98 encodes them);
+ * center < 0 selects n/2.  Writes the amplitude array (DC at [0,0], A >= 0
+ * known, -1 unknown, <= -2 upper bound -A-2).  No device is touched. */
+int spe_prepare_pattern(const float* intensities, int n, int center_x, int center_y, int use_bounds,
+                        float* amplitudes_out);
+
+/* Creates an engine for n x n patterns on CUDA device `device`.
+ * Replaces the constructor GPU_context::GPU_context (gpu_context.h:17-84):
+ * one stream, twiddle tables instead of a cuFFT plan. */
+int spe_create(int n, int device, spe_engine** out);
+int spe_destroy(spe_engine* e);
+
+/* Run on a caller's CUDA stream (cudaStream_t passed as void*; NULL
+ * restores the engine's own stream). */
+int spe_set_stream(spe_engine* e, void* cuda_stream);
+int spe_get_stream(spe_engine* e, void** cuda_stream);
+
+/* Amplitudes of the pattern (output of spe_prepare_pattern), n x n float.
+ * Replaces GPU_context::set_pattern / get_pattern (gpu_context.cu:610-674). */
+int spe_set_amplitudes(spe_engine* e, const float* amplitudes);
+int spe_get_amplitudes(spe_engine* e, float* amplitudes);
+
+/* Population capacity in individuals (device memory for density, support
+ * and scratch).  Existing contents up to min(old, new) are kept. */
+int spe_reserve(spe_engine* e, int capacity);
+int spe_capacity(spe_engine* e, int* capacity);
+
+/* Copies `count` individuals between host and the resident population.
+ * Replaces GPU_context::set_density/set_support/get_density/get_support
+ * (gpu_context.cu:598-692), batched.  density: count * n * n complex64
+ * (2 floats each); support: count * n * n int32.  Either may be NULL to
+ * skip it.  spe_download synchronises. */
+int spe_upload(spe_engine* e, int first, int count, const float* density, const int32_t* support);
+int spe_download(spe_engine* e, int first, int count, float* density, int32_t* support);
+
+/* Device addresses of the resident population (density, support), for
+ * callers that keep data on the GPU. */
+int spe_device_buffers(spe_engine* e, void** density, void** support);
+
+/* Iterative algorithms on [first, first+count): GPU_context::HIO / RAAR / ER
+ * (gpu_context.cu:778-902) and Solver::HIO / RAAR / ER
+ * (src/solver.cpp:360-411).  Same semantics: the previous iterate is reset
+ * to the current density at entry, `iterations` update steps, then one
+ * trailing modulus projection.  reality: the phase constraint (Solver's
+ * reality, src/solver.h:85). */
+int spe_hio(spe_engine* e, int first, int count, int iterations, float beta, float reality);
+int spe_raar(spe_engine* e, int first, int count, int iterations, float beta, float reality);
+int spe_er(spe_engine* e, int first, int count, int iterations, float reality);
+
+/* Shrink-wrap support updates: GPU_context::SW / SWA
+ * (gpu_context.cu:906-1027), Solver::SW / SWA (src/solver.cpp:414-450).
+ * SW keeps pixels whose blurred modulus is >= threshold * max; SWA keeps the
+ * `pixels` largest (ties included).  The density is unchanged.  SWA clamps
+ * `pixels` to [1, n*n] (the reference reads past its buffer for 0). */
+int spe_sw(spe_engine* e, int first, int count, float sigma, float threshold, float reality);
+int spe_swa(spe_engine* e, int first, int count, float sigma, int pixels, float reality);
+
+/* Error metrics and symmetry of each individual: Solver::Evaluate
+ * (src/solver.cpp:541-558) with GPU_context::get_error and get_symmetry
+ * (gpu_context.cu:1030-1134, 1378-1463).  metrics: `count` entries. */
+int spe_evaluate(spe_engine* e, int first, int count, float reality, float realpen, spe_metrics* metrics);
+
+/* Solver::Sequence (src/solver.cpp:454-487): runs the op list `nrep` times
+ * on every individual, then evaluates.  metrics may be NULL. */
+int spe_sequence(spe_engine* e, int first, int count, const spe_op* ops, int nops, int nrep, float reality,
+                 float realpen, spe_metrics* metrics);
+
+/* Waits for all work queued on the engine's stream. */
+int spe_synchronize(spe_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPE_ENGINE_H */

@@ -1,0 +1,699 @@
+"""CPU oracle for the SPRING phase-retrieval iteration engine.
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import this
+module, and only as the checker: nothing in the shipped engine calls it.
+
+This is a restatement, in numpy, of the reference's per-individual GPU path
+(MasterSPP/S_SPI_SPRING ``src/gpu/gpu_context.cu`` and ``src/solver.cpp``).  The
+reference has no CPU implementation of the path (its ``CPU_context`` is an empty
+stub, ``src/cpu/cpu_context.h:14-29``), so the oracle follows the GPU kernels'
+arithmetic.  Precision policy:
+
+* transforms and pointwise arithmetic run in float64 (``numpy.fft``);
+* the branch decisions that the reference takes on float32 values (the
+  phase gate of ``apply_support_*``, ``atan2`` based on float32 operands) are
+  taken on float32-rounded copies, compared against the same double
+  thresholds the reference's code forms (``(1.f-real)*M_PI`` is a double);
+* host-side encodings that the reference computes in float32 on the CPU
+  (``Solver::set_boundaries`` / ``Solver::prepare``) are reproduced in float32
+  in the reference's order of operations, so they are bit-exact.
+
+Parity status: the reference repository carries no golden vectors, fixtures or
+known-answer tests for this path, and its only implementation needs a GPU plus
+cuFFT, so it cannot be executed where this oracle is validated.  Parity of the
+iteration arithmetic is therefore UNPINNED against the reference's own outputs;
+the oracle is validated by known-answer tests (delta / plane-wave FFTs, P_M
+idempotence, ER fixed points, SW on a known disc, crossover with all-zero /
+all-one crossmaps) and by the RNG draw sequence, which is pinned to the C++
+standard library definitions the reference calls.
+
+FFT sign map (``gpu_context.cu:748-774``): ``get_ft`` = cuFFT INVERSE
+(exponent +i, unnormalised) = ``N*N*ifft2``; ``get_ift`` = cuFFT FORWARD
+followed by ``/N^2`` (``normalize``, ``gpu_context.cu:65-77``) = ``fft2/N^2``.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+M_PI = math.pi
+
+
+# ----------------------------------------------------------------------------
+# FFT conventions
+# ----------------------------------------------------------------------------
+def ft(x):
+    """cuFFT CUFFT_INVERSE, unnormalised (``gpu_context.cu:748-754``)."""
+    n0, n1 = x.shape[-2:]
+    return np.fft.ifft2(x) * (n0 * n1)
+
+
+def ift_raw(x):
+    """cuFFT CUFFT_FORWARD without the normalisation (``gpu_context.cu:938``)."""
+    return np.fft.fft2(x)
+
+
+def ift(x):
+    """cuFFT CUFFT_FORWARD followed by ``normalize`` (``gpu_context.cu:757-764``)."""
+    n0, n1 = x.shape[-2:]
+    return np.fft.fft2(x) / float(n0 * n1)
+
+
+# ----------------------------------------------------------------------------
+# Phase gate thresholds, formed exactly as the reference's kernels form them
+# ----------------------------------------------------------------------------
+def gate_thresholds(real, kind="er"):
+    """Return (upper, lower) double thresholds of the phase gate.
+
+    ``apply_support_er`` / ``apply_support_hio`` / ``get_real_error_gpu`` use
+    ``(1.f-real_flag)*M_PI`` on both sides (``gpu_context.cu:530,553,407``);
+    ``apply_support_raar`` uses ``(1.-real_flag)*M_PI`` on the upper side and
+    ``(1.f-real_flag)*M_PI`` on the lower side (``gpu_context.cu:582``).
+    ``real`` is a float32 kernel argument.
+    """
+    r32 = np.float32(real)
+    lo = float(np.float32(np.float32(1.0) - r32)) * M_PI
+    if kind == "raar":
+        hi = (1.0 - float(r32)) * M_PI
+    else:
+        hi = lo
+    return hi, lo
+
+
+def phase_f32(z):
+    """``atan2(y, x)`` evaluated on float32 operands, as the kernels do."""
+    z32 = np.asarray(z).astype(np.complex64)
+    return np.arctan2(z32.imag, z32.real).astype(np.float64)
+
+
+def gate_er(z, S, real, kind="er"):
+    """Effective support of ``apply_support_er``: S * [|arg z| <= (1-real)pi]
+    (``gpu_context.cu:519-537``).  Returns a float64 array of 0/1 (S values are
+    used as-is, as ``FLOAT tempsupp = support[i]``)."""
+    hi, lo = gate_thresholds(real, kind)
+    ph = phase_f32(z)
+    g = np.asarray(S, dtype=np.float64).copy()
+    g[(ph > hi) | (ph < -lo)] = 0.0
+    return g
+
+
+# ----------------------------------------------------------------------------
+# Kernels (pointwise)
+# ----------------------------------------------------------------------------
+def sub_intensities(F, A):
+    """Masked modulus projection P_M (``gpu_context.cu:79-111``).
+
+    A >= 0: F <- A F/|F| (|F| == 0: F <- A (cos phi, sin phi), phi = atan2 of
+    the signed zeros); A < -1.5 and |F| > -A-2: F <- (-A-2) F/|F|; else F."""
+    F = np.array(F, dtype=np.complex128, copy=True)
+    A = np.asarray(A, dtype=np.float64)
+    m = np.abs(F)
+    known = A >= 0.0
+    nz = known & (m > 0.0)
+    F[nz] = A[nz] * F[nz] / m[nz]
+    z = known & ~(m > 0.0)
+    if np.any(z):
+        ph = np.arctan2(F[z].imag, F[z].real)
+        F[z] = A[z] * np.cos(ph) + 1j * A[z] * np.sin(ph)
+    bound = ~known & (A < -1.5)
+    bmod = -A - 2.0
+    clip = bound & (m > bmod)
+    F[clip] = bmod[clip] * F[clip] / m[clip]
+    return F
+
+
+def modulus_projection(rho, A):
+    """rho -> F^-1 P_M F rho (``gpu_context.cu:788-797``)."""
+    return ift(sub_intensities(ft(rho), A))
+
+
+def apply_support_er(rho, S, real):
+    """``gpu_context.cu:519-537``."""
+    return rho * gate_er(rho, S, real, "er")
+
+
+def apply_support_hio(rho_p, S, buf, beta, real):
+    """HIO update (``gpu_context.cu:540-565``); returns (rho, buffer)."""
+    t = gate_er(rho_p, S, real, "er")
+    beta = float(np.float32(beta))
+    out = (buf - beta * rho_p) * (1.0 - t) + rho_p * t
+    return out, out.copy()
+
+
+def apply_support_raar(rho_p, S, buf, beta, real):
+    """RAAR update (``gpu_context.cu:568-593``); returns (rho, buffer)."""
+    hi, lo = gate_thresholds(real, "raar")
+    refl = 2.0 * rho_p - buf
+    ph = phase_f32(refl)
+    outside = (ph > hi) | (ph < -lo) | (np.asarray(S) == 0)
+    beta = float(np.float32(beta))
+    out = rho_p.copy()
+    out[outside] = beta * buf[outside] + (1.0 - 2.0 * beta) * rho_p[outside]
+    return out, out.copy()
+
+
+# ----------------------------------------------------------------------------
+# Iterative algorithms (GPU_context::HIO/RAAR/ER, ``gpu_context.cu:778-902``)
+# ----------------------------------------------------------------------------
+def _iterate(rho, S, A, n, update):
+    rho = np.asarray(rho, dtype=np.complex128)
+    buf = rho.copy()                       # buffer <- rho at entry (:782)
+    for _ in range(int(n)):
+        rp = modulus_projection(rho, A)    # FFT, P_M, FFT, /N^2 (:788-797)
+        rho, buf = update(rp, buf)         # apply_support_* (:799)
+    return modulus_projection(rho, A)      # trailing projection (:803-812)
+
+
+def hio(rho, S, A, n, beta, real=0.0):
+    return _iterate(rho, S, A, n,
+                    lambda rp, buf: apply_support_hio(rp, S, buf, beta, real))
+
+
+def raar(rho, S, A, n, beta, real=0.0):
+    return _iterate(rho, S, A, n,
+                    lambda rp, buf: apply_support_raar(rp, S, buf, beta, real))
+
+
+def er(rho, S, A, n, real=0.0):
+    return _iterate(rho, S, A, n,
+                    lambda rp, buf: (apply_support_er(rp, S, real), buf))
+
+
+# ----------------------------------------------------------------------------
+# Shrink-wrap (GPU_context::SW / SWA, ``gpu_context.cu:906-1027``)
+# ----------------------------------------------------------------------------
+def smooth_coeff(N, sigma):
+    """``smooth_intensities`` factor exp(-r^2/sigma_ft^2), r from the corner
+    origin (``gpu_context.cu:199-218``); sigma_ft = FLOAT(N)/sigma/M_PI
+    (``:935``)."""
+    sft = float(np.float32(float(np.float32(N) / np.float32(sigma)) / M_PI))
+    k = np.arange(N)
+    k = np.where(k >= N // 2, k - N, k)
+    r2 = (k[None, :] ** 2 + k[:, None] ** 2).astype(np.float64)
+    return np.exp(-r2 / (sft * sft))
+
+
+def blurred_modulus(rho, A, sigma):
+    """|FFT_fwd(smooth(FFT_inv(|P_M rho|)))| without normalisation."""
+    N = rho.shape[-1]
+    pm = modulus_projection(rho, A)
+    g = ft(np.abs(pm)) * smooth_coeff(N, sigma)
+    return np.abs(ift_raw(g))
+
+
+def sw(rho, S, A, sigma, threshold, real=0.0):
+    """Support <- [blur >= thr * max blur]; rho unchanged (``:906-953``)."""
+    m = blurred_modulus(rho, A, sigma)
+    thr = float(np.float32(threshold))
+    return (m >= m.max() * thr).astype(np.int32)
+
+
+def swa_threshold(m, spixels):
+    """k-th largest blurred value (``gpu_context.cu:1004-1015``).
+
+    The reference indexes one past the end when ``spixels <= 0``; the engine
+    clamps ``spixels`` to at least 1 and so does the oracle."""
+    flat = np.sort(m.ravel())
+    n = flat.size
+    k = int(min(max(int(spixels), 1), n))
+    return flat[n - k]
+
+
+def swa(rho, S, A, sigma, spixels, real=0.0):
+    m = blurred_modulus(rho, A, sigma)
+    return (m >= swa_threshold(m, spixels)).astype(np.int32)
+
+
+# ----------------------------------------------------------------------------
+# Error metrics (GPU_context::get_error, ``gpu_context.cu:1030-1134``)
+# ----------------------------------------------------------------------------
+@dataclass
+class ErrorTerms:
+    error_fourier: float
+    error_real: float
+    complexsum: float
+    modulesum: float
+
+
+def get_error(rho, S, A, real=0.0):
+    rho = np.asarray(rho, dtype=np.complex128)
+    A = np.asarray(A, dtype=np.float64)
+    rs = apply_support_er(rho, S, real)             # :1040
+    F = ft(rs)                                      # :1050
+    known = A >= 0
+    mF = np.abs(F)
+    err_f = np.sum((A[known] - mF[known]) ** 2)     # get_error_gpu :352-385
+    norm_f = np.sum(A[known] ** 2)
+    fmax = mF.max()                                 # get_max_module :435-461
+    msum = np.sum(np.abs(rs))                       # get_module_sum(exp=1) :219-246
+    r2 = ift(sub_intensities(F, A))                 # :1097-1102
+    # get_real_error_gpu (:386-434), including the product in the x term
+    hi, lo = gate_thresholds(real, "er")
+    ph = phase_f32(r2)
+    t = np.asarray(S, dtype=np.float64).copy()
+    t[(ph > hi) | (ph < -lo)] = 0.0
+    xs = r2.real * t
+    ys = r2.imag * t
+    norm_r = np.sum(np.abs(r2) ** 2)
+    diff = (r2.imag - ys) ** 2 + (r2.real * xs) ** 2
+    err_r = np.sum(diff[np.asarray(S) == 0])
+    return ErrorTerms(math.sqrt(err_f / norm_f), math.sqrt(err_r / norm_r),
+                      float(fmax), float(msum))
+
+
+def bandpass(N, minr, maxr):
+    """Radial weight of ``multiply`` (``gpu_context.cu:1157-1200``); the kernel
+    multiplies by its square."""
+    k = np.arange(N, dtype=np.float64)
+    k = np.where(k >= N // 2, k - N, k)
+    radius = np.sqrt(k[None, :] ** 2 + k[:, None] ** 2)
+    f32 = np.float32
+    sigtot = float(f32(float(f32(N)) * float(f32(minr)) / 2.0 + 1e-12))
+    sig = float(f32(sigtot / 10.0))
+    eff = radius - (sigtot - sig)
+    with np.errstate(over="ignore", divide="ignore", invalid="ignore"):
+        coeff = np.where(eff > 0, 1.0 - np.exp(-eff * eff / (sig * sig)), 0.0)
+    sigtotmax = float(f32(float(f32(N)) * float(f32(maxr)) / 2.0 + 1e-12))
+    sigmax = float(f32(sigtotmax / 10.0))
+    effm = radius - (sigtotmax - sigmax)
+    coeffm = np.where(effm > 0, np.exp(-effm * effm / (sigmax * sigmax)), 1.0)
+    c = coeff * coeffm
+    return c * c
+
+
+def _normalize_ft_shift(D):
+    """``normalize_ft_shift`` with exponent 1 (``gpu_context.cu:37-50``):
+    identity except NaN where |D| == 0."""
+    D = D.copy()
+    z = np.abs(D) == 0
+    D[z] = np.nan
+    return D
+
+
+def _corr_peaks(D, Dref, A, minr, maxr):
+    """Both cross-correlations of ``get_shift`` (``gpu_context.cu:1261-1306``):
+    returns (max1, idx1, max2, idx2) of |FFT_fwd(.)|^2 (first index of the
+    maximum in raster order)."""
+    N = D.shape[-1]
+    w = bandpass(N, minr, maxr)
+    masked = np.asarray(A) < 0
+    c1 = np.conj(D) * Dref * w
+    c2 = D * Dref * w
+    c1[masked] = 0
+    c2[masked] = 0
+    out = []
+    for c in (c1, c2):
+        v = np.abs(ift_raw(c)) ** 2
+        flat = v.ravel()
+        finite = np.where(np.isnan(flat), -np.inf, flat)
+        i = int(np.argmax(finite))
+        mx = finite[i]
+        if not mx > 0:
+            i, mx = 0, 0.0
+        out += [float(mx), i]
+    return tuple(out)
+
+
+def get_symmetry(rho, A, symmin=0.0, symmax=1.0):
+    """``GPU_context::get_symmetry`` (``gpu_context.cu:1378-1463``)."""
+    D = _normalize_ft_shift(ft(np.abs(rho)))
+    m1, _, m2, _ = _corr_peaks(D, D, A, symmin, symmax)
+    if m1 == 0:
+        return float("nan")
+    return math.sqrt(m2 / m1)
+
+
+def evaluate(rho, S, A, real=0.0, realpen=0.0):
+    """``Solver::Evaluate`` per individual (``solver.cpp:541-558``)."""
+    e = get_error(rho, S, A, real)
+    sym = get_symmetry(rho, A, 0.0, 1.0)
+    reality = 1.0 - e.complexsum / e.modulesum
+    return dict(error=e.error_fourier * (1.0 + realpen * reality),
+                error_fourier=e.error_fourier, error_real=e.error_real,
+                complexsum=e.complexsum, modulesum=e.modulesum,
+                reality=reality, symmetry=sym)
+
+
+# ----------------------------------------------------------------------------
+# Alignment (get_shift / reshift / shift, ``gpu_context.cu:1226-1371``)
+# ----------------------------------------------------------------------------
+def get_shift(rho, rho_ref, A, minr=0.0, maxr=2.0, normalize_ft=True):
+    """Returns (shiftx, shifty, shiftphase, flip).
+
+    ``normalize_ft`` selects the ``set_ref_density``/``get_shift`` flavour
+    (normalize_ft_shift applied to both spectra, ``:663,1255``) versus the
+    ``prepare_parents``/``reshift_parent`` flavour (not applied, ``:1680,1567``).
+    The global phases come from the complex sums of the densities."""
+    N = rho.shape[-1]
+    D = ft(np.abs(rho))
+    Dr = ft(np.abs(rho_ref))
+    if normalize_ft:
+        D = _normalize_ft_shift(D)
+        Dr = _normalize_ft_shift(Dr)
+    m1, i1, m2, i2 = _corr_peaks(D, Dr, A, minr, maxr)
+    s = np.sum(rho)
+    sr = np.sum(rho_ref)
+    ph = math.atan2(s.imag, s.real)
+    phr = math.atan2(sr.imag, sr.real)
+    if m1 >= m2:
+        return i1 % N, i1 // N, phr - ph, False
+    # C++: -maxindex2 % N and -maxindex2 / N truncate toward zero
+    return -(i2 % N), -(i2 // N), phr + ph, True
+
+
+def shift(rho, S, shiftx, shifty, shiftphase, flip):
+    """``shift`` kernel (``gpu_context.cu:1329-1357``)."""
+    N = rho.shape[-1]
+    iy, ix = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    nx = ix + shiftx
+    ny = iy + shifty
+    nx = np.where(nx < 0, nx + N, nx)
+    nx = np.where(nx >= N, nx - N, nx)
+    ny = np.where(ny < 0, ny + N, ny)
+    ny = np.where(ny >= N, ny - N, ny)
+    new = nx + ny * N
+    if flip:
+        new = N * N - 1 - new
+    mod = np.abs(rho)
+    ph = np.arctan2(rho.imag, rho.real)
+    if flip:
+        ph = -ph
+    ph = ph + shiftphase
+    out = np.zeros(N * N, dtype=np.complex128)
+    sout = np.zeros(N * N, dtype=np.int32)
+    out[new.ravel()] = (mod * np.exp(1j * ph)).ravel()
+    sout[new.ravel()] = np.asarray(S).ravel()
+    return out.reshape(N, N), sout.reshape(N, N)
+
+
+def reshift(rho, S, rho_ref, A, minr=0.0, maxr=2.0):
+    """``Solver::Reshift_rec`` (``solver.cpp:490-507``)."""
+    sx, sy, sp, fl = get_shift(rho, rho_ref, A, minr, maxr, normalize_ft=True)
+    return shift(rho, S, sx, sy, sp, fl)
+
+
+# ----------------------------------------------------------------------------
+# Population averages (``solver.cpp:564-686``)
+# ----------------------------------------------------------------------------
+def _navg(fraction, P):
+    n = int(np.float32(np.float32(fraction) * np.float32(P)))
+    return min(max(n, 1), P)
+
+
+def sorted_indexes(errors):
+    """Order of ``std::sort`` with ``a.error < b.error``; errors are assumed
+    distinct (ties are resolved by libstdc++'s introsort in the engine)."""
+    return [int(i) for i in np.argsort(np.asarray(errors, dtype=np.float32),
+                                       kind="stable")]
+
+
+def get_average(rhos, supports, errors, fraction):
+    P = len(rhos)
+    n = _navg(fraction, P)
+    idx = sorted_indexes(errors)[:n]
+    dens = np.zeros_like(np.asarray(rhos[0], dtype=np.complex64))
+    supp = np.zeros(np.asarray(supports[0]).shape, dtype=np.int64)
+    for i in idx:                               # add kernels, sorted order
+        dens = (dens + np.asarray(rhos[i], dtype=np.complex64)).astype(np.complex64)
+        supp = supp + np.asarray(supports[i])
+    norm = np.float32(1.0 / float(np.float32(n)))
+    dens = (dens * norm).astype(np.complex64)
+    return dens, (supp > 0).astype(np.int32)
+
+
+def get_average_module(rhos, errors, ft_flag=True, fraction=1.0):
+    P = len(rhos)
+    n = _navg(fraction, P)
+    idx = sorted_indexes(errors)[:n]
+    acc = np.zeros(np.asarray(rhos[0]).shape, dtype=np.float64)
+    for i in idx:
+        x = np.asarray(rhos[i], dtype=np.complex128)
+        acc += np.abs(ft(x) if ft_flag else x)
+    return acc * float(np.float32(1.0 / float(np.float32(n))))
+
+
+# ----------------------------------------------------------------------------
+# Pattern encoding (Solver::set_boundaries + Solver::prepare), float32 exact
+# ----------------------------------------------------------------------------
+def prepare_pattern(intensities, center=(-1, -1), use_bounds=True):
+    """Restates ``Solver::Solver`` (``solver.cpp:9-22``): set_boundaries
+    (``:209-289``) then prepare (``:173-206``).  Square patterns only, as the
+    reference (``solver.cpp:37``).  float32 arithmetic in the reference's
+    order, so the result is bit-exact."""
+    f32 = np.float32
+    pat = np.array(intensities, dtype=np.float32).reshape(-1).copy()
+    d0 = int(np.asarray(intensities).shape[0])
+    d1 = int(np.asarray(intensities).shape[1])
+    c0, c1 = int(center[0]), int(center[1])
+    if c0 < 0:
+        c0 = d0 // 2
+    if c1 < 0:
+        c1 = d1 // 2
+    # ---- set_boundaries
+    profsize = int(math.sqrt(c0 * c0 + c1 * c1) / 1.0) + 10
+    radprof = np.zeros(profsize, np.float32)
+    radstd = np.zeros(profsize, np.float32)
+    counts = np.zeros(profsize, np.float32)
+    totc = np.zeros(profsize, np.float32)
+    totsat = np.zeros(profsize, np.float32)
+    jj, ii = np.meshgrid(np.arange(d1), np.arange(d0), indexing="ij")
+    dist = np.sqrt(((jj - c1) ** 2 + (ii - c0) ** 2).astype(np.float64)).astype(np.float32)
+    # std::round on float: half away from zero
+    dcent = np.floor(dist.astype(np.float64) + 0.5).astype(np.int64).ravel()
+    # One contribution per (pixel, span) in the C++ loop order (pixel-major,
+    # span -1, 0, +1); ufunc.at applies them sequentially in float32.
+    d3 = (dcent[:, None] + np.array([-1, 0, 1])[None, :]).ravel()
+    v3 = np.repeat(pat, 3)
+    ok3 = (d3 < profsize) & (d3 >= 0)
+    pos = ok3 & (v3 >= 0)
+    np.add.at(radprof, d3[pos], v3[pos])
+    np.add.at(radstd, d3[pos], (v3[pos] * v3[pos]).astype(np.float32))
+    np.add.at(counts, d3[pos], f32(1.0))
+    sat = ok3 & (v3 < -1.5)
+    np.add.at(totsat, d3[sat], f32(1.0))
+    np.add.at(totc, d3[ok3], f32(1.0))
+    ok = (counts.astype(np.float64) > totc.astype(np.float64) * 0.66) & \
+         (totsat.astype(np.float64) <= totc.astype(np.float64) * 0.05) & \
+         (totc.astype(np.float64) > 40)
+    rp = np.where(ok, radprof / np.where(ok, counts, f32(1)), f32(-1)).astype(np.float32)
+    mean_sq = (radstd / np.where(ok, counts, f32(1))).astype(np.float32)
+    rstd = np.sqrt(np.abs((mean_sq - (rp * rp).astype(np.float32)).astype(np.float32))).astype(np.float32)
+    rstd = np.where(ok, rstd, radstd).astype(np.float32)
+    neg = pat < 0
+    d = dcent
+    inrange = neg & (d < profsize) & (d > 0)
+    dd = np.where(inrange, d, 0)
+    cand = inrange & (rp[dd] >= 0) & (pat < -0.5) & (pat > -1.5)
+    bound = (rp[dd].astype(np.float64) + 1.0 * rstd[dd].astype(np.float64)).astype(np.float32)
+    newv = (-2.0 - np.sqrt(bound).astype(np.float32).astype(np.float64)).astype(np.float32)
+    pat = np.where(cand, newv, np.where(inrange, f32(-1.0), pat)).astype(np.float32)
+    # ---- prepare
+    out = np.empty_like(pat)
+    src = pat.reshape(d1, d0)            # [j][i], i fastest
+    for j in range(d1):
+        ky = j - c1
+        if ky < 0:
+            ky += d1
+        i = np.arange(d0)
+        kx = i - c0
+        kx = np.where(kx < 0, kx + d0, kx)
+        v = src[j]
+        nv = np.where(v >= 0, np.sqrt(np.maximum(v, 0)).astype(np.float32),
+                      v if use_bounds else f32(-1.0))
+        out[kx + d0 * ky] = nv
+    return out.reshape(d1, d0)
+
+
+# ----------------------------------------------------------------------------
+# Random numbers: std::mt19937 + std::uniform_real_distribution<float>
+# ----------------------------------------------------------------------------
+class MT19937:
+    """Mersenne Twister MT19937 (Matsumoto & Nishimura 1998), 32-bit output,
+    seeded like ``std::mt19937(seed)``."""
+
+    def __init__(self, seed):
+        self.mt = [0] * 624
+        self.mt[0] = int(seed) & 0xFFFFFFFF
+        for i in range(1, 624):
+            prev = self.mt[i - 1]
+            self.mt[i] = (1812433253 * (prev ^ (prev >> 30)) + i) & 0xFFFFFFFF
+        self.idx = 624
+
+    def _twist(self):
+        mt = self.mt
+        for i in range(624):
+            y = (mt[i] & 0x80000000) | (mt[(i + 1) % 624] & 0x7FFFFFFF)
+            v = mt[(i + 397) % 624] ^ (y >> 1)
+            if y & 1:
+                v ^= 0x9908B0DF
+            mt[i] = v
+        self.idx = 0
+
+    def __call__(self):
+        if self.idx >= 624:
+            self._twist()
+        y = self.mt[self.idx]
+        self.idx += 1
+        y ^= y >> 11
+        y ^= (y << 7) & 0x9D2C5680
+        y ^= (y << 15) & 0xEFC60000
+        y ^= y >> 18
+        return y & 0xFFFFFFFF
+
+
+class ContextRNG:
+    """``Context::rand`` (``src/context.h:13-18``): a float uniform in [0,1)
+    from ``generate_canonical<float,24>`` over one 32-bit draw, scaled as
+    ``u*(max-min)+min`` in float."""
+
+    def __init__(self, seed):
+        self.g = MT19937(seed)
+
+    def uniform(self):
+        f32 = np.float32
+        r = f32(f32(self.g()) / f32(4294967296.0))
+        if r >= f32(1.0):
+            r = np.nextafter(f32(1.0), f32(0.0), dtype=np.float32)
+        return r
+
+    def rand(self, lo=0.0, hi=1.0):
+        f32 = np.float32
+        lo = f32(lo)
+        hi = f32(hi)
+        return f32(f32(self.uniform() * f32(hi - lo)) + lo)
+
+
+# ----------------------------------------------------------------------------
+# Crossover (Solver::Crossover + GPU_context, ``solver.cpp:716-817``)
+# ----------------------------------------------------------------------------
+@dataclass
+class CrossDraw:
+    p1: int
+    p2: int
+    p3: int
+    crossft: bool
+    squaresizex: int
+    squaresizey: int
+    crosssizex: int
+    crosssizey: int
+    offsetx: int
+    offsety: int
+    rotangle: float
+    crossmap: np.ndarray
+
+
+def suppdim_of(best_support, N):
+    """``solver.cpp:724-729``."""
+    n = int(np.sum(np.asarray(best_support, dtype=np.int64)))
+    f32 = np.float32
+    sd = f32(2.0 * math.sqrt(float(f32(n)) / M_PI))
+    if sd < 4.0:
+        sd = f32(4.0)
+    if sd > N / 4.0:
+        sd = f32(N / 4.0)
+    return sd
+
+
+def draw_crossover(rng, P, order, suppdim, N, crossbalance, crossexp, crossftin):
+    """The per-child draws of ``solver.cpp:750-801``, in the reference's order.
+    ``order`` is the error-sorted index list."""
+    f32 = np.float32
+    draws = []
+    for _ in range(P):
+        u = rng.rand(0, 1)
+        extracted = int(f32(f32(float(u) ** float(f32(crossexp))) * f32(P)))
+        p1 = order[extracted]
+        p2 = int(rng.rand(0, f32(P - 0.0001)))
+        p3 = int(rng.rand(0, f32(P - 0.0001)))
+        cft = bool(rng.rand(0, 1) < f32(crossftin))
+        if cft:
+            lo = f32(math.ceil(float(f32(f32(N) / suppdim))))
+            hi = f32(math.ceil(float(f32(f32(N) / f32(4.0)))))
+        else:
+            lo = f32(float(suppdim) / 10.0 + 1.0)
+            hi = f32(float(suppdim) / 2.0)
+        ssx = int(rng.rand(lo, hi))
+        ssy = int(rng.rand(lo, hi))
+        csx = (N + ssx - 1) // ssx + 1
+        csy = (N + ssy - 1) // ssy + 1
+        ox = int(rng.rand(0, ssx))
+        oy = int(rng.rand(0, ssy))
+        rot = rng.rand(0, M_PI)
+        cmap = np.zeros(csx * csy, np.int32)
+        for i in range(csx * csy):
+            if rng.rand(0, 1) < f32(crossbalance):
+                cmap[i] = 1
+        draws.append(CrossDraw(p1, p2, p3, cft, ssx, ssy, csx, csy, ox, oy,
+                               float(rot), cmap))
+    return draws
+
+
+def crossmap_index(N, csx, ssx, ssy, ox, oy, rot, crosssym):
+    """Cell index of each pixel in ``cross_density`` (``gpu_context.cu:1717-1739``),
+    evaluated in float32."""
+    f32 = np.float32
+    iy, ix = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    x = np.where(ix >= N // 2, ix - N, ix)
+    y = np.where(iy >= N // 2, iy - N, iy)
+    radius = np.sqrt((x * x + y * y).astype(np.float32)).astype(np.float32)
+    radius = np.where(radius.astype(np.float64) >= N / 2.0, f32(N // 2 - 1), radius).astype(np.float32)
+    angle = np.arctan2(y.astype(np.float32), x.astype(np.float32)).astype(np.float32)
+    if crosssym:
+        angle = np.where(angle < 0, (angle.astype(np.float64) + M_PI).astype(np.float32), angle)
+    angle = (angle + f32(rot)).astype(np.float32)
+    xr = np.trunc((np.cos(angle) * radius).astype(np.float32)).astype(np.int64) + N // 2
+    yr = np.trunc((np.sin(angle) * radius).astype(np.float32)).astype(np.int64) + N // 2
+    cx = (xr + ox) // ssx
+    cy = (yr + oy) // ssy
+    return cx + cy * csx
+
+
+def new_individual(self_rho, self_S, p1, S1, p2, S2, p3, S3, avg_rho, A,
+                   avg_mod, draw, crossdiff, use_average, crosssym, real):
+    """``GPU_context::get_new_individual`` (``gpu_context.cu:2044-2117``) on
+    densities that are already aligned to p1.  Returns (density, support)."""
+    N = self_rho.shape[-1]
+    d1 = apply_support_er(p1, S1, real)
+    d0 = apply_support_er(self_rho, self_S, real)
+    d2 = apply_support_er(p2, S2, real)
+    d3 = apply_support_er(p3, S3, real)
+    davg = np.asarray(avg_rho, dtype=np.complex128)
+    if draw.crossft:
+        d0, d1, d2, d3, davg = ft(d0), ft(d1), ft(d2), ft(d3), ft(davg)
+    cell = crossmap_index(N, draw.crosssizex, draw.squaresizex, draw.squaresizey,
+                          draw.offsetx, draw.offsety, draw.rotangle, crosssym)
+    do = draw.crossmap[cell] == 1
+    out = d0.copy()
+    if draw.crossft:
+        d1t = d1.copy()
+        mod1 = np.abs(d1)
+        A = np.asarray(A)
+        ua = float(np.float32(use_average))
+        if ua > 0:
+            avgm = (avg_mod + np.abs(davg)) * 0.5
+            newm = avgm * ua + (1.0 - ua) * mod1
+            sel = (A < 0) & (mod1 > 0)
+            d1t[sel] = d1[sel] * newm[sel] / mod1[sel]
+        elif ua < 0:
+            loc = abs(ua)
+            maxm = avg_mod
+            minm = np.abs(davg)
+            newm = mod1.copy()
+            lo = newm < minm
+            hi = ~lo & (newm > maxm)
+            newm[lo] = minm[lo] * loc + newm[lo] * (1.0 - loc)
+            newm[hi] = maxm[hi] * loc + newm[hi] * (1.0 - loc)
+            sel = (A < 0) & (mod1 > 0)
+            d1t[sel] = d1[sel] * newm[sel] / mod1[sel]
+        out[do] = d1t[do] + crossdiff * (d2[do] - d3[do])
+    else:
+        out[do] = d1[do] + crossdiff * (d2[do] - d3[do])
+    s = np.asarray(S1, np.int64) + np.asarray(S2, np.int64) * np.asarray(S3, np.int64) * np.asarray(self_S, np.int64)
+    s = (s > 0.5).astype(np.int32)
+    if draw.crossft:
+        out = ift(out)
+    out = apply_support_er(out, s, real)
+    return out, s

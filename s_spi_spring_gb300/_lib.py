@@ -1,0 +1,223 @@
+"""ctypes binding of the engine's C ABI (``include/spe_engine.h``).
+
+The shared library is built in-tree (``s_spi_spring_gb300/_build/libspe.so``,
+see ``build.py``).  Loading fails loudly when it is missing: there is no
+CPU fallback for the engine.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent / "_build" / "libspe.so"
+_lock = threading.Lock()
+_lib = None
+
+SPE_OK = 0
+SPE_OP_HIO, SPE_OP_RAAR, SPE_OP_ER, SPE_OP_SW, SPE_OP_SWA = range(5)
+
+# Every symbol the header declares, with (restype, argtypes).
+_vp = C.c_void_p
+_i = C.c_int
+_f = C.c_float
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int32)
+
+
+class SpeOp(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("iterations", C.c_int32), ("beta", C.c_float),
+                ("sigma", C.c_float), ("threshold", C.c_float), ("pixels", C.c_int32)]
+
+
+class SpeMetrics(C.Structure):
+    _fields_ = [("error", C.c_float), ("error_fourier", C.c_float), ("error_real", C.c_float),
+                ("reality", C.c_float), ("modulesum", C.c_float), ("complexsum", C.c_float),
+                ("symmetry", C.c_float)]
+
+
+SIGNATURES = {
+    "spe_last_error": (C.c_char_p, []),
+    "spe_version": (_i, []),
+    "spe_prepare_pattern": (_i, [_fp, _i, _i, _i, _i, _fp]),
+    "spe_create": (_i, [_i, _i, C.POINTER(_vp)]),
+    "spe_destroy": (_i, [_vp]),
+    "spe_set_stream": (_i, [_vp, _vp]),
+    "spe_get_stream": (_i, [_vp, C.POINTER(_vp)]),
+    "spe_set_amplitudes": (_i, [_vp, _fp]),
+    "spe_get_amplitudes": (_i, [_vp, _fp]),
+    "spe_reserve": (_i, [_vp, _i]),
+    "spe_capacity": (_i, [_vp, C.POINTER(_i)]),
+    "spe_upload": (_i, [_vp, _i, _i, _fp, _ip]),
+    "spe_download": (_i, [_vp, _i, _i, _fp, _ip]),
+    "spe_device_buffers": (_i, [_vp, C.POINTER(_vp), C.POINTER(_vp)]),
+    "spe_hio": (_i, [_vp, _i, _i, _i, _f, _f]),
+    "spe_raar": (_i, [_vp, _i, _i, _i, _f, _f]),
+    "spe_er": (_i, [_vp, _i, _i, _i, _f]),
+    "spe_sw": (_i, [_vp, _i, _i, _f, _f, _f]),
+    "spe_swa": (_i, [_vp, _i, _i, _f, _i, _f]),
+    "spe_evaluate": (_i, [_vp, _i, _i, _f, _f, C.POINTER(SpeMetrics)]),
+    "spe_sequence": (_i, [_vp, _i, _i, C.POINTER(SpeOp), _i, _i, _f, _f, C.POINTER(SpeMetrics)]),
+    "spe_synchronize": (_i, [_vp]),
+}
+
+
+class EngineError(RuntimeError):
+    """A C ABI call returned a non-zero status."""
+
+    def __init__(self, fn, code, msg):
+        super().__init__(f"{fn} failed ({code}): {msg}")
+        self.code = code
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def load():
+    """Load (once) and return the engine library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not _LIB_PATH.exists():
+            raise ImportError(
+                f"engine library {_LIB_PATH} is not built; run "
+                "`python -c 'import __graft_entry__ as g; g.build()'` first")
+        lib = C.CDLL(str(_LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def call(name, *args):
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != SPE_OK:
+        raise EngineError(name, rc, lib.spe_last_error().decode())
+    return rc
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(_fp) if a is not None else None
+
+
+def iptr(a: np.ndarray):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+class Engine:
+    """Owning handle of one engine (one pattern size, one device)."""
+
+    def __init__(self, n: int, device: int = 0):
+        h = _vp()
+        call("spe_create", int(n), int(device), C.byref(h))
+        self.h = h
+        self.n = int(n)
+        self.device = int(device)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().spe_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- pattern / population ------------------------------------------------
+    def set_amplitudes(self, amp):
+        amp = np.ascontiguousarray(amp, dtype=np.float32)
+        assert amp.shape == (self.n, self.n)
+        call("spe_set_amplitudes", self.h, fptr(amp))
+
+    def get_amplitudes(self):
+        out = np.empty((self.n, self.n), np.float32)
+        call("spe_get_amplitudes", self.h, fptr(out))
+        return out
+
+    def reserve(self, capacity: int):
+        call("spe_reserve", self.h, int(capacity))
+
+    @property
+    def capacity(self) -> int:
+        c = C.c_int()
+        call("spe_capacity", self.h, C.byref(c))
+        return c.value
+
+    def upload(self, first, density=None, support=None):
+        d = None if density is None else np.ascontiguousarray(density, dtype=np.complex64)
+        s = None if support is None else np.ascontiguousarray(support, dtype=np.int32)
+        arr = d if d is not None else s
+        count = arr.size // (self.n * self.n)
+        self.reserve(first + count)
+        call("spe_upload", self.h, int(first), int(count),
+             None if d is None else d.view(np.float32).ctypes.data_as(_fp), iptr(s))
+
+    def download(self, first, count, density=True, support=True):
+        d = np.empty((count, self.n, self.n), np.complex64) if density else None
+        s = np.empty((count, self.n, self.n), np.int32) if support else None
+        call("spe_download", self.h, int(first), int(count),
+             None if d is None else d.view(np.float32).ctypes.data_as(_fp), iptr(s))
+        return d, s
+
+    def set_stream(self, stream_handle: int | None):
+        call("spe_set_stream", self.h, _vp(stream_handle or 0))
+
+    def device_buffers(self):
+        d, s = _vp(), _vp()
+        call("spe_device_buffers", self.h, C.byref(d), C.byref(s))
+        return d.value, s.value
+
+    # -- algorithms ------------------------------------------------------------
+    def hio(self, first, count, iterations, beta, reality=0.0):
+        call("spe_hio", self.h, int(first), int(count), int(iterations), float(beta), float(reality))
+
+    def raar(self, first, count, iterations, beta, reality=0.0):
+        call("spe_raar", self.h, int(first), int(count), int(iterations), float(beta), float(reality))
+
+    def er(self, first, count, iterations, reality=0.0):
+        call("spe_er", self.h, int(first), int(count), int(iterations), float(reality))
+
+    def sw(self, first, count, sigma, threshold, reality=0.0):
+        call("spe_sw", self.h, int(first), int(count), float(sigma), float(threshold), float(reality))
+
+    def swa(self, first, count, sigma, pixels, reality=0.0):
+        call("spe_swa", self.h, int(first), int(count), float(sigma), int(pixels), float(reality))
+
+    def evaluate(self, first, count, reality=0.0, realpen=0.0):
+        m = (SpeMetrics * max(count, 1))()
+        call("spe_evaluate", self.h, int(first), int(count), float(reality), float(realpen), m)
+        return [metrics_dict(m[i]) for i in range(count)]
+
+    def sequence(self, first, count, ops, nrep=1, reality=0.0, realpen=0.0, evaluate=True):
+        arr = (SpeOp * max(len(ops), 1))(*ops)
+        m = (SpeMetrics * max(count, 1))() if evaluate else None
+        call("spe_sequence", self.h, int(first), int(count), arr, len(ops), int(nrep),
+             float(reality), float(realpen), m)
+        return [metrics_dict(m[i]) for i in range(count)] if evaluate else None
+
+    def synchronize(self):
+        call("spe_synchronize", self.h)
+
+
+def metrics_dict(m: SpeMetrics) -> dict:
+    return {k: float(getattr(m, k)) for k, _ in SpeMetrics._fields_}
+
+
+def prepare_pattern(intensities, center=(-1, -1), use_bounds=True):
+    """Host pattern encoding of the reference Solver (see include/spe_engine.h)."""
+    x = np.ascontiguousarray(intensities, dtype=np.float32)
+    if x.ndim != 2 or x.shape[0] != x.shape[1]:
+        raise ValueError("patterns must be square 2D arrays")
+    out = np.empty_like(x)
+    call("spe_prepare_pattern", fptr(x), x.shape[0], int(center[0]), int(center[1]),
+         int(bool(use_bounds)), fptr(out))
+    return out

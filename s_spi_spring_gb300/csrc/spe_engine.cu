@@ -1,0 +1,629 @@
+// Engine object, small helper kernels and the C ABI (include/spe_engine.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/spe_engine.h"
+#include "spe_internal.h"
+
+namespace spe {
+const SizeOps* size_ops_16();
+const SizeOps* size_ops_32();
+const SizeOps* size_ops_64();
+const SizeOps* size_ops_128();
+const SizeOps* size_ops_256();
+const SizeOps* size_ops_384();
+const SizeOps* size_ops_512();
+const SizeOps* size_ops_768();
+const SizeOps* size_ops_1024();
+const SizeOps* size_ops_2048();
+
+const SizeOps* size_ops(int n) {
+  switch (n) {
+    case 16: return size_ops_16();
+    case 32: return size_ops_32();
+    case 64: return size_ops_64();
+    case 128: return size_ops_128();
+    case 256: return size_ops_256();
+    case 384: return size_ops_384();
+    case 512: return size_ops_512();
+    case 768: return size_ops_768();
+    case 1024: return size_ops_1024();
+    case 2048: return size_ops_2048();
+    default: return nullptr;
+  }
+}
+
+constexpr int NRED = 4;
+
+// ---------------------------------------------------------------------------
+// helper kernels
+// ---------------------------------------------------------------------------
+
+// out[i*ostride + oslot] = sum / max over the tpi partials of individual i
+__global__ void k_reduce(const double* __restrict__ part, int count, int tpi, int k, int is_max, double* out,
+                         int ostride, int oslot) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const double* p = part + (size_t)i * tpi * NRED + k;
+  double a = p[0];
+  for (int t = 1; t < tpi; ++t) a = is_max ? fmax(a, p[(size_t)t * NRED]) : a + p[(size_t)t * NRED];
+  out[(size_t)i * ostride + oslot] = a;
+}
+
+// per-individual argmax over the per-CTA (value, index) pairs
+__global__ void k_reduce_peak(const double* __restrict__ part, int count, int tpi, double* out, int ostride,
+                              int oslot) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const double* p = part + (size_t)i * tpi * NRED;
+  double m = p[0], idx = p[1];
+  for (int t = 1; t < tpi; ++t) {
+    const double v = p[(size_t)t * NRED], j = p[(size_t)t * NRED + 1];
+    if (v > m || (v == m && j < idx)) {
+      m = v;
+      idx = j;
+    }
+  }
+  if (!(m > 0.0)) idx = 0.0;  // no value above 0: the reference keeps index 0
+  out[(size_t)i * ostride + oslot] = m;
+  out[(size_t)i * ostride + oslot + 1] = idx;
+}
+
+// support <- M >= max * thr (cut_support, gpu_context.cu:466-481)
+__global__ void k_threshold_rel(const float* __restrict__ M, int* __restrict__ S, const double* __restrict__ mx,
+                                int mstride, float thr, size_t npix, int first, int count) {
+  const size_t total = npix * (size_t)count;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i / npix);
+    const size_t gi = (size_t)first * npix + i;
+    const float t = (float)mx[(size_t)p * mstride] * thr;
+    S[gi] = (M[gi] >= t) ? 1 : 0;
+  }
+}
+
+// support <- M >= thr_p (cut_support with an absolute threshold, gpu_context.cu:484-499)
+__global__ void k_threshold_abs(const float* __restrict__ M, int* __restrict__ S, const uint32_t* __restrict__ state,
+                                size_t npix, int first, int count) {
+  const size_t total = npix * (size_t)count;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int p = (int)(i / npix);
+    const size_t gi = (size_t)first * npix + i;
+    S[gi] = (M[gi] >= __uint_as_float(state[2 * p])) ? 1 : 0;
+  }
+}
+
+// ---- k-th largest magnitude per individual (radix select over the float
+// bit patterns; magnitudes are >= 0 so their bits order like the values).
+// state[2p] = prefix found so far, state[2p+1] = rank still to find.
+__global__ void k_select_init(uint32_t* state, int count, uint32_t k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) {
+    state[2 * i] = 0u;
+    state[2 * i + 1] = k;
+  }
+}
+
+__global__ void k_select_hist(const float* __restrict__ M, size_t npix, int first, int blocks_per_ind,
+                              const uint32_t* __restrict__ state, uint32_t* __restrict__ hist, int shift) {
+  __shared__ uint32_t h[256];
+  for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0u;
+  __syncthreads();
+  const int p = blockIdx.x / blocks_per_ind;
+  const int part = blockIdx.x % blocks_per_ind;
+  const uint32_t prefix = state[2 * p];
+  const uint32_t himask = (shift >= 24) ? 0u : (0xffffffffu << (shift + 8));
+  const uint32_t* keys = reinterpret_cast<const uint32_t*>(M + (size_t)(first + p) * npix);
+  const size_t chunk = (npix + blocks_per_ind - 1) / blocks_per_ind;
+  const size_t lo = part * chunk, hi = (lo + chunk < npix) ? lo + chunk : npix;
+  for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const uint32_t key = keys[i];
+    if ((key & himask) == (prefix & himask)) atomicAdd(&h[(key >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < 256; b += blockDim.x)
+    if (h[b]) atomicAdd(&hist[(size_t)p * 256 + b], h[b]);
+}
+
+__global__ void k_select_pick(uint32_t* __restrict__ state, uint32_t* __restrict__ hist, int count, int shift) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= count) return;
+  uint32_t* h = hist + (size_t)p * 256;
+  uint32_t k = state[2 * p + 1];
+  uint32_t cum = 0;
+  int bin = 0;
+  for (int b = 255; b >= 0; --b) {
+    if (cum + h[b] >= k) {
+      bin = b;
+      break;
+    }
+    cum += h[b];
+  }
+  state[2 * p] |= ((uint32_t)bin << shift);
+  state[2 * p + 1] = k - cum;
+  for (int b = 0; b < 256; ++b) h[b] = 0u;
+}
+
+}  // namespace spe
+
+// ---------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------
+struct spe_engine {
+  int dev = 0;
+  int n = 0;
+  size_t npix = 0;
+  const spe::SizeOps* ops = nullptr;
+  cudaStream_t own = nullptr;
+  cudaStream_t st = nullptr;
+  int cap = 0;
+  bool have_amp = false;
+  float* A = nullptr;
+  float2* tw = nullptr;
+  float2* rho = nullptr;
+  int* S = nullptr;
+  float2* T = nullptr;
+  float2* T2 = nullptr;
+  float* M = nullptr;
+  double* partials = nullptr;  // 5 regions of cap * tpi * NRED
+  double* red = nullptr;       // cap * 16
+  double* red_host = nullptr;  // pinned
+  uint32_t* sel_state = nullptr;
+  uint32_t* sel_hist = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? SPE_ERR_NOMEM : SPE_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                             \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+float largest_float_not_above(double t) {
+  float f = (float)t;
+  if ((double)f > t) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+
+// apply_support_er / _hio and get_real_error_gpu compare against
+// (1.f-real)*M_PI on both sides (gpu_context.cu:530,553,407)
+spe::Gate gate_er(float real) {
+  const double t = (double)(1.f - real) * M_PI;
+  const float f = largest_float_not_above(t);
+  return spe::Gate{f, f};
+}
+// apply_support_raar: (1.-real)*M_PI above, (1.f-real)*M_PI below (:582)
+spe::Gate gate_raar(float real) {
+  const double hi = (1.0 - (double)real) * M_PI;
+  const double lo = (double)(1.f - real) * M_PI;
+  return spe::Gate{largest_float_not_above(hi), largest_float_not_above(lo)};
+}
+
+int check_range(spe_engine* e, int first, int count) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  if (first < 0 || count < 0 || (long long)first + count > e->cap)
+    return fail(SPE_ERR_INVALID, "range [%d, %d) outside the population capacity %d", first, first + count, e->cap);
+  return SPE_OK;
+}
+
+int need_amp(spe_engine* e) {
+  if (!e->have_amp) return fail(SPE_ERR_STATE, "amplitudes not set (spe_set_amplitudes)");
+  return SPE_OK;
+}
+
+spe::Ctx make_ctx(spe_engine* e, int first, int count) {
+  spe::Ctx c;
+  c.n = e->n;
+  c.first = first;
+  c.count = count;
+  c.st = e->st;
+  c.rho = e->rho;
+  c.S = e->S;
+  c.T = e->T;
+  c.T2 = e->T2;
+  c.M = e->M;
+  c.A = e->A;
+  c.tw = e->tw;
+  c.partials = e->partials;
+  c.red = e->red;
+  return c;
+}
+
+size_t region(spe_engine* e) { return (size_t)e->cap * e->ops->tiles_per_individual * spe::NRED; }
+
+int reduce(spe_engine* e, const double* part, int count, int k, int is_max, int slot) {
+  const int tpi = e->ops->tiles_per_individual;
+  spe::k_reduce<<<(count + 127) / 128, 128, 0, e->st>>>(part, count, tpi, k, is_max, e->red, 16, slot);
+  CK(cudaGetLastError(), "reduce launch");
+  return SPE_OK;
+}
+
+int reduce_peak(spe_engine* e, const double* part, int count, int slot) {
+  const int tpi = e->ops->tiles_per_individual;
+  spe::k_reduce_peak<<<(count + 127) / 128, 128, 0, e->st>>>(part, count, tpi, e->red, 16, slot);
+  CK(cudaGetLastError(), "peak reduce launch");
+  return SPE_OK;
+}
+
+int fetch_red(spe_engine* e, int count) {
+  CK(cudaMemcpyAsync(e->red_host, e->red, (size_t)count * 16 * sizeof(double), cudaMemcpyDeviceToHost, e->st),
+     "copy results");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  return SPE_OK;
+}
+
+void free_population(spe_engine* e) {
+  cudaFree(e->rho);
+  cudaFree(e->S);
+  cudaFree(e->T);
+  cudaFree(e->T2);
+  cudaFree(e->M);
+  cudaFree(e->partials);
+  cudaFree(e->red);
+  cudaFreeHost(e->red_host);
+  cudaFree(e->sel_state);
+  cudaFree(e->sel_hist);
+  e->rho = nullptr;
+  e->S = nullptr;
+  e->T = e->T2 = nullptr;
+  e->M = nullptr;
+  e->partials = e->red = nullptr;
+  e->red_host = nullptr;
+  e->sel_state = e->sel_hist = nullptr;
+}
+
+int do_iterate(spe_engine* e, int first, int count, int upd, int iters, float beta, float real) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if ((rc = need_amp(e))) return rc;
+  if (iters < 0) return fail(SPE_ERR_INVALID, "negative iteration count");
+  if (count == 0) return SPE_OK;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  const spe::Gate g = (upd == 1) ? gate_raar(real) : gate_er(real);
+  CK(e->ops->iterate(make_ctx(e, first, count), upd, iters, beta, g), "iteration kernels");
+  return SPE_OK;
+}
+
+int do_shrinkwrap(spe_engine* e, int first, int count, float sigma, bool absolute, float threshold, int pixels) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if ((rc = need_amp(e))) return rc;
+  if (count == 0) return SPE_OK;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  // FLOAT sigmaft = FLOAT(npixels)/sigma/M_PI  (gpu_context.cu:935)
+  const float sft = (float)((double)((float)e->n / sigma) / M_PI);
+  spe::Ctx c = make_ctx(e, first, count);
+  CK(e->ops->blur_magnitude(c, sft), "shrink-wrap kernels");
+  const unsigned grid = 152 * 8;
+  if (!absolute) {
+    if ((rc = reduce(e, e->partials, count, 0, 1, 0))) return rc;
+    spe::k_threshold_rel<<<grid, 256, 0, e->st>>>(e->M, e->S, e->red, 16, threshold, e->npix, first, count);
+    CK(cudaGetLastError(), "threshold launch");
+    return SPE_OK;
+  }
+  long long k = pixels;
+  if (k > (long long)e->npix) k = (long long)e->npix;
+  if (k < 1) k = 1;
+  spe::k_select_init<<<(count + 127) / 128, 128, 0, e->st>>>(e->sel_state, count, (uint32_t)k);
+  CK(cudaGetLastError(), "select init");
+  CK(cudaMemsetAsync(e->sel_hist, 0, (size_t)count * 256 * sizeof(uint32_t), e->st), "memset");
+  const int bpi = (int)std::max<size_t>(1, std::min<size_t>(256, e->npix / 4096));
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    spe::k_select_hist<<<(unsigned)count * bpi, 256, 0, e->st>>>(e->M, e->npix, first, bpi, e->sel_state,
+                                                                 e->sel_hist, shift);
+    CK(cudaGetLastError(), "select histogram");
+    spe::k_select_pick<<<(count + 127) / 128, 128, 0, e->st>>>(e->sel_state, e->sel_hist, count, shift);
+    CK(cudaGetLastError(), "select pick");
+  }
+  spe::k_threshold_abs<<<grid, 256, 0, e->st>>>(e->M, e->S, e->sel_state, e->npix, first, count);
+  CK(cudaGetLastError(), "threshold launch");
+  return SPE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* spe_last_error(void) { return g_err.c_str(); }
+
+int spe_version(void) { return 100; }
+
+int spe_prepare_pattern(const float* intensities, int n, int center_x, int center_y, int use_bounds,
+                        float* amplitudes_out) {
+  if (!intensities || !amplitudes_out || n <= 0) return fail(SPE_ERR_INVALID, "invalid pattern arguments");
+  spe::prepare_pattern(intensities, n, center_x, center_y, use_bounds != 0, amplitudes_out);
+  return SPE_OK;
+}
+
+int spe_create(int n, int device, spe_engine** out) {
+  if (!out) return fail(SPE_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  const spe::SizeOps* ops = spe::size_ops(n);
+  if (!ops)
+    return fail(SPE_ERR_UNSUPPORTED,
+                "pattern side %d has no compiled FFT plan (supported: 16,32,64,128,256,384,512,768,1024,2048)", n);
+  int ndev = 0;
+  CK(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+  if (device < 0 || device >= ndev) return fail(SPE_ERR_INVALID, "device %d not present (%d devices)", device, ndev);
+  CK(cudaSetDevice(device), "cudaSetDevice");
+  spe_engine* e = new spe_engine();
+  e->dev = device;
+  e->n = n;
+  e->npix = (size_t)n * n;
+  e->ops = ops;
+  cudaError_t err = cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking);
+  if (err != cudaSuccess) {
+    delete e;
+    return cuda_fail(err, "stream");
+  }
+  e->st = e->own;
+  std::vector<float2> tw(n);
+  for (int m = 0; m < n; ++m) {
+    const double a = 2.0 * M_PI * (double)m / (double)n;
+    tw[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  err = cudaMalloc(&e->tw, n * sizeof(float2));
+  if (err == cudaSuccess) err = cudaMalloc(&e->A, e->npix * sizeof(float));
+  if (err == cudaSuccess) err = cudaMemcpy(e->tw, tw.data(), n * sizeof(float2), cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) {
+    cudaFree(e->tw);
+    cudaFree(e->A);
+    cudaStreamDestroy(e->own);
+    delete e;
+    return cuda_fail(err, "engine allocation");
+  }
+  *out = e;
+  return SPE_OK;
+}
+
+int spe_destroy(spe_engine* e) {
+  if (!e) return SPE_OK;
+  cudaSetDevice(e->dev);
+  cudaStreamSynchronize(e->st);
+  free_population(e);
+  cudaFree(e->A);
+  cudaFree(e->tw);
+  cudaStreamDestroy(e->own);
+  delete e;
+  return SPE_OK;
+}
+
+int spe_set_stream(spe_engine* e, void* stream) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  e->st = stream ? (cudaStream_t)stream : e->own;
+  return SPE_OK;
+}
+
+int spe_get_stream(spe_engine* e, void** stream) {
+  if (!e || !stream) return fail(SPE_ERR_INVALID, "null argument");
+  *stream = (void*)e->st;
+  return SPE_OK;
+}
+
+int spe_set_amplitudes(spe_engine* e, const float* amp) {
+  if (!e || !amp) return fail(SPE_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  CK(cudaMemcpyAsync(e->A, amp, e->npix * sizeof(float), cudaMemcpyHostToDevice, e->st), "upload amplitudes");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  e->have_amp = true;
+  return SPE_OK;
+}
+
+int spe_get_amplitudes(spe_engine* e, float* amp) {
+  if (!e || !amp) return fail(SPE_ERR_INVALID, "null argument");
+  int rc = need_amp(e);
+  if (rc) return rc;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  CK(cudaMemcpyAsync(amp, e->A, e->npix * sizeof(float), cudaMemcpyDeviceToHost, e->st), "download amplitudes");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  return SPE_OK;
+}
+
+int spe_reserve(spe_engine* e, int capacity) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  if (capacity < 0) return fail(SPE_ERR_INVALID, "negative capacity");
+  if (capacity <= e->cap) return SPE_OK;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  spe_engine t = *e;  // new buffers
+  t.cap = capacity;
+  const size_t np = (size_t)capacity * e->npix;
+  const size_t tpi = e->ops->tiles_per_individual;
+  cudaError_t err = cudaSuccess;
+  t.rho = nullptr;
+  t.S = nullptr;
+  t.T = t.T2 = nullptr;
+  t.M = nullptr;
+  t.partials = t.red = nullptr;
+  t.red_host = nullptr;
+  t.sel_state = t.sel_hist = nullptr;
+  if (err == cudaSuccess) err = cudaMalloc(&t.rho, np * sizeof(float2));
+  if (err == cudaSuccess) err = cudaMalloc(&t.S, np * sizeof(int));
+  if (err == cudaSuccess) err = cudaMalloc(&t.T, np * sizeof(float2));
+  if (err == cudaSuccess) err = cudaMalloc(&t.T2, np * sizeof(float2));
+  if (err == cudaSuccess) err = cudaMalloc(&t.M, np * sizeof(float));
+  if (err == cudaSuccess) err = cudaMalloc(&t.partials, 5 * (size_t)capacity * tpi * spe::NRED * sizeof(double));
+  if (err == cudaSuccess) err = cudaMalloc(&t.red, (size_t)capacity * 16 * sizeof(double));
+  if (err == cudaSuccess) err = cudaMallocHost(&t.red_host, (size_t)capacity * 16 * sizeof(double));
+  if (err == cudaSuccess) err = cudaMalloc(&t.sel_state, (size_t)capacity * 2 * sizeof(uint32_t));
+  if (err == cudaSuccess) err = cudaMalloc(&t.sel_hist, (size_t)capacity * 256 * sizeof(uint32_t));
+  if (err == cudaSuccess && e->cap > 0) {
+    const size_t old = (size_t)e->cap * e->npix;
+    err = cudaMemcpy(t.rho, e->rho, old * sizeof(float2), cudaMemcpyDeviceToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(t.S, e->S, old * sizeof(int), cudaMemcpyDeviceToDevice);
+  }
+  if (err != cudaSuccess) {
+    free_population(&t);
+    return cuda_fail(err, "population allocation");
+  }
+  free_population(e);
+  e->cap = t.cap;
+  e->rho = t.rho;
+  e->S = t.S;
+  e->T = t.T;
+  e->T2 = t.T2;
+  e->M = t.M;
+  e->partials = t.partials;
+  e->red = t.red;
+  e->red_host = t.red_host;
+  e->sel_state = t.sel_state;
+  e->sel_hist = t.sel_hist;
+  return SPE_OK;
+}
+
+int spe_capacity(spe_engine* e, int* capacity) {
+  if (!e || !capacity) return fail(SPE_ERR_INVALID, "null argument");
+  *capacity = e->cap;
+  return SPE_OK;
+}
+
+int spe_upload(spe_engine* e, int first, int count, const float* density, const int32_t* support) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if (count == 0) return SPE_OK;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  const size_t off = (size_t)first * e->npix, np = (size_t)count * e->npix;
+  if (density)
+    CK(cudaMemcpyAsync(e->rho + off, density, np * sizeof(float2), cudaMemcpyHostToDevice, e->st), "upload density");
+  if (support)
+    CK(cudaMemcpyAsync(e->S + off, support, np * sizeof(int), cudaMemcpyHostToDevice, e->st), "upload support");
+  return SPE_OK;
+}
+
+int spe_download(spe_engine* e, int first, int count, float* density, int32_t* support) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  const size_t off = (size_t)first * e->npix, np = (size_t)count * e->npix;
+  if (density && count)
+    CK(cudaMemcpyAsync(density, e->rho + off, np * sizeof(float2), cudaMemcpyDeviceToHost, e->st),
+       "download density");
+  if (support && count)
+    CK(cudaMemcpyAsync(support, e->S + off, np * sizeof(int), cudaMemcpyDeviceToHost, e->st), "download support");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  return SPE_OK;
+}
+
+int spe_device_buffers(spe_engine* e, void** density, void** support) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  if (density) *density = e->rho;
+  if (support) *support = e->S;
+  return SPE_OK;
+}
+
+int spe_hio(spe_engine* e, int first, int count, int iterations, float beta, float reality) {
+  return do_iterate(e, first, count, 0, iterations, beta, reality);
+}
+int spe_raar(spe_engine* e, int first, int count, int iterations, float beta, float reality) {
+  return do_iterate(e, first, count, 1, iterations, beta, reality);
+}
+int spe_er(spe_engine* e, int first, int count, int iterations, float reality) {
+  return do_iterate(e, first, count, 2, iterations, 0.f, reality);
+}
+
+int spe_sw(spe_engine* e, int first, int count, float sigma, float threshold, float reality) {
+  (void)reality;  // the reference's SW takes `real` but never uses it (gpu_context.cu:906-953)
+  return do_shrinkwrap(e, first, count, sigma, false, threshold, 0);
+}
+
+int spe_swa(spe_engine* e, int first, int count, float sigma, int pixels, float reality) {
+  (void)reality;
+  return do_shrinkwrap(e, first, count, sigma, true, 0.f, pixels);
+}
+
+int spe_evaluate(spe_engine* e, int first, int count, float reality, float realpen, spe_metrics* m) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if ((rc = need_amp(e))) return rc;
+  if (count > 0 && !m) return fail(SPE_ERR_INVALID, "null metrics pointer");
+  if (count == 0) return SPE_OK;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  spe::Ctx c = make_ctx(e, first, count);
+  const size_t R = region(e);
+  double *p1 = e->partials, *p2 = p1 + R, *p3 = p2 + R, *p4 = p3 + R, *p5 = p4 + R;
+  CK(e->ops->error_terms(c, gate_er(reality), p1, p2, p3), "error kernels");
+  // red slots: 0 modulesum, 1 err_f, 2 norm_f, 3 max|F|, 4 err_r, 5 norm_r,
+  //            6/7 peak1 (value, index), 8/9 peak2
+  if ((rc = reduce(e, p1, count, 0, 0, 0))) return rc;
+  if ((rc = reduce(e, p2, count, 0, 0, 1))) return rc;
+  if ((rc = reduce(e, p2, count, 1, 0, 2))) return rc;
+  if ((rc = reduce(e, p2, count, 2, 1, 3))) return rc;
+  if ((rc = reduce(e, p3, count, 0, 0, 4))) return rc;
+  if ((rc = reduce(e, p3, count, 1, 0, 5))) return rc;
+  // get_symmetry (gpu_context.cu:1378-1463): D = FFT+(|rho|) normalised,
+  // peaks of |FFT-(conj(D) D w)|^2 and |FFT-(D D w)|^2, band 0..1
+  CK(e->ops->abs_spectrum(c, e->T2), "symmetry spectrum");
+  CK(e->ops->corr_peak(c, e->T2, e->T2, e->npix, first, -1, 0.f, 1.f, 1, 1, p4), "symmetry correlation");
+  if ((rc = reduce_peak(e, p4, count, 6))) return rc;
+  CK(e->ops->corr_peak(c, e->T2, e->T2, e->npix, first, +1, 0.f, 1.f, 1, 1, p5), "symmetry correlation");
+  if ((rc = reduce_peak(e, p5, count, 8))) return rc;
+  if ((rc = fetch_red(e, count))) return rc;
+  for (int i = 0; i < count; ++i) {
+    const double* r = e->red_host + (size_t)i * 16;
+    // GPU_context::get_error (gpu_context.cu:1126-1131) in float, as the reference
+    const float ef = (float)r[1], nf = (float)r[2], er = (float)r[4], nr = (float)r[5];
+    spe_metrics& o = m[i];
+    o.error_fourier = (float)std::pow((double)(ef / nf), 0.5);
+    o.error_real = (float)std::pow((double)(er / nr), 0.5);
+    o.complexsum = (float)r[3];
+    o.modulesum = (float)r[0];
+    o.symmetry = std::sqrt((float)r[8] / (float)r[6]);
+    // Solver::Evaluate (src/solver.cpp:552-554)
+    o.reality = (float)(1. - (double)(o.complexsum / o.modulesum));
+    o.error = (float)((double)o.error_fourier * (1. + (double)(realpen * o.reality)));
+  }
+  return SPE_OK;
+}
+
+int spe_sequence(spe_engine* e, int first, int count, const spe_op* ops, int nops, int nrep, float reality,
+                 float realpen, spe_metrics* metrics) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if (nops > 0 && !ops) return fail(SPE_ERR_INVALID, "null op list");
+  for (int r = 0; r < nrep; ++r) {
+    for (int k = 0; k < nops; ++k) {
+      const spe_op& op = ops[k];
+      switch (op.kind) {
+        case SPE_OP_HIO: rc = spe_hio(e, first, count, op.iterations, op.beta, reality); break;
+        case SPE_OP_RAAR: rc = spe_raar(e, first, count, op.iterations, op.beta, reality); break;
+        case SPE_OP_ER: rc = spe_er(e, first, count, op.iterations, reality); break;
+        case SPE_OP_SW: rc = spe_sw(e, first, count, op.sigma, op.threshold, reality); break;
+        case SPE_OP_SWA: rc = spe_swa(e, first, count, op.sigma, op.pixels, reality); break;
+        default: return fail(SPE_ERR_INVALID, "unknown op kind %d", op.kind);
+      }
+      if (rc) return rc;
+    }
+  }
+  if (metrics) return spe_evaluate(e, first, count, reality, realpen, metrics);
+  return SPE_OK;
+}
+
+int spe_synchronize(spe_engine* e) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  return SPE_OK;
+}
+
+}  // extern "C"

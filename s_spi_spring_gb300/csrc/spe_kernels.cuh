@@ -1,0 +1,569 @@
+// Fused row / column pass kernels of the phase-retrieval iteration.
+//
+// Layout in HBM: the population is P individuals of N x N complex64
+// (interleaved re/im, x fastest, i = x + y*N), individual p at offset p*N*N.
+// A 2D transform is a row pass (transforms along x, 16 rows per CTA) and a
+// column pass (transforms along y, 16 columns per CTA).  One iteration of
+// HIO / RAAR / ER is
+//   column pass: T -> FFT+ (y) -> masked modulus projection -> FFT- (y) -> T
+//   row pass:    T -> FFT- (x) -> /N^2 -> support update with rho, S -> rho
+//                  -> FFT+ (x) -> T
+// so the iterate rho and the half-transformed scratch T are each read and
+// written once per iteration, with every FFT stage, the projection and the
+// update fused into the two passes.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "spe_fft.cuh"
+
+namespace spe {
+
+enum { AX_ROWS = 0, AX_COLS = 1 };
+
+// per-CTA partial results: NRED doubles per CTA (sums in fixed order later)
+constexpr int NRED = 4;
+
+// ---------------------------------------------------------------------------
+// point operations shared by the ops
+// ---------------------------------------------------------------------------
+
+// Phase gate of apply_support_* (reference gpu_context.cu:526-530): the
+// reference compares the float atan2 against a double threshold
+// (1-real)*M_PI; the host passes the largest float not above that double, so
+// the float comparison below takes the same decision.
+__device__ __forceinline__ bool phase_out(float2 v, float thi, float tlo) {
+  const float ph = atan2f(v.y, v.x);
+  return (ph > thi) || (ph < -tlo);
+}
+
+// Masked modulus projection P_M (reference sub_intensities,
+// gpu_context.cu:79-111).  a >= 0: known amplitude; a < -1.5: upper bound
+// -a-2; otherwise unknown.
+__device__ __forceinline__ float2 project(float2 F, float a) {
+  const float m = sqrtf(F.y * F.y + F.x * F.x);
+  if (a >= 0.f) {
+    if (m > 0.f) {
+      const float s = __fdiv_rn(a, m);
+      return make_float2(F.x * s, F.y * s);
+    }
+    float sn, cs;
+    sincosf(atan2f(F.y, F.x), &sn, &cs);
+    return make_float2(a * cs, a * sn);
+  }
+  if (a < -1.5f) {
+    const float b = -a - 2.f;
+    if (m > b) {
+      const float s = __fdiv_rn(b, m);
+      return make_float2(F.x * s, F.y * s);
+    }
+  }
+  return F;
+}
+
+__device__ __forceinline__ float cabsf2(float2 v) { return sqrtf(v.y * v.y + v.x * v.x); }
+
+// ---------------------------------------------------------------------------
+// block reduction of NRED values per CTA into partials[blockIdx.x*NRED + k]
+// (k < NSUM: sums, k >= NSUM: maxima)
+// ---------------------------------------------------------------------------
+template <int NT, int NSUM, int NMAX>
+__device__ __forceinline__ void block_reduce_store(double* __restrict__ partials, const double (&v)[NRED]) {
+  static_assert(NSUM + NMAX <= NRED, "too many reduction values");
+  constexpr int NW = NT / 32;
+  __shared__ double red[NRED][NW > 0 ? NW : 1];
+  double x[NRED];
+#pragma unroll
+  for (int k = 0; k < NRED; ++k) x[k] = v[k];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int k = 0; k < NSUM + NMAX; ++k) {
+      const double o = __shfl_down_sync(0xffffffffu, x[k], off);
+      x[k] = (k < NSUM) ? x[k] + o : fmax(x[k], o);
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) red[k][wid] = x[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NSUM + NMAX; ++k) {
+      double a = red[k][0];
+      for (int w = 1; w < NW; ++w) a = (k < NSUM) ? a + red[k][w] : fmax(a, red[k][w]);
+      partials[(size_t)blockIdx.x * NRED + k] = a;
+    }
+  }
+}
+
+// block argmax of (value, raster index): larger value wins, ties go to the
+// lower index; writes partials[blockIdx.x*NRED + {0,1}] = {value, index}
+template <int NT>
+__device__ __forceinline__ void block_argmax_store(double* __restrict__ partials, float mx, int idx) {
+  constexpr int NW = NT / 32;
+  __shared__ float rv[NW > 0 ? NW : 1];
+  __shared__ int ri[NW > 0 ? NW : 1];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float ov = __shfl_down_sync(0xffffffffu, mx, off);
+    const int oi = __shfl_down_sync(0xffffffffu, idx, off);
+    if (ov > mx || (ov == mx && oi < idx)) {
+      mx = ov;
+      idx = oi;
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    rv[wid] = mx;
+    ri[wid] = idx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = rv[0];
+    int i = ri[0];
+    for (int w = 1; w < NW; ++w) {
+      if (rv[w] > m || (rv[w] == m && ri[w] < i)) {
+        m = rv[w];
+        i = ri[w];
+      }
+    }
+    partials[(size_t)blockIdx.x * NRED + 0] = m;
+    partials[(size_t)blockIdx.x * NRED + 1] = (double)i;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the pass kernel
+// ---------------------------------------------------------------------------
+struct TileGeom {
+  int p;   // individual (absolute slot)
+  int y0;  // first row of the tile (row pass) or 0
+  int x0;  // first column of the tile (column pass) or 0
+};
+
+template <int N, int AXIS>
+__device__ __forceinline__ TileGeom tile_geom(int first) {
+  constexpr int W = TileW<N>::value;
+  constexpr int TPI = N / W;  // tiles per individual
+  TileGeom g;
+  g.p = first + blockIdx.x / TPI;
+  const int t = blockIdx.x % TPI;
+  g.y0 = (AXIS == AX_ROWS) ? t * W : 0;
+  g.x0 = (AXIS == AX_COLS) ? t * W : 0;
+  return g;
+}
+
+// Element i of the staging loops -> (l, c) of the tile and (y, x) of the
+// individual.  Row pass: consecutive i walk along x of one row (coalesced
+// global access, conflict-free swizzled stores).  Column pass: consecutive i
+// walk along the W columns of one row, then down the rows.
+template <int N, int AXIS>
+__device__ __forceinline__ void stage_coords(int i, const TileGeom& g, int& l, int& c, int& y, int& x) {
+  constexpr int W = TileW<N>::value;
+  if (AXIS == AX_ROWS) {
+    c = i / N;
+    l = i - c * N;
+    y = g.y0 + c;
+    x = l;
+  } else {
+    l = i / W;
+    c = i - l * W;
+    y = l;
+    x = g.x0 + c;
+  }
+}
+
+template <int N, int AXIS, class Op>
+__global__ void __launch_bounds__(TileW<N>::value * Plan<N>::TPT)
+    pass_kernel(const Op op, const float2* __restrict__ twg) {
+  constexpr int W = TileW<N>::value;
+  constexpr int NT = W * Plan<N>::TPT;
+  extern __shared__ float2 smem[];
+  float2* tile = smem;
+  float2* tw = smem + N * W;
+  for (int i = threadIdx.x; i < N; i += NT) tw[i] = twg[i];
+
+  const TileGeom g = tile_geom<N, AXIS>(op.first);
+  const size_t base = (size_t)g.p * N * N;
+  typename Op::Acc acc;
+
+#pragma unroll 4
+  for (int i = threadIdx.x; i < N * W; i += NT) {
+    int l, c, y, x;
+    stage_coords<N, AXIS>(i, g, l, c, y, x);
+    tile[tidx<W>(l, c)] = op.load(base + (size_t)y * N + x, g.p, y, x, acc);
+  }
+  __syncthreads();
+  if constexpr (Op::FFT1 != 0) Plan<N>::template run<W, Op::FFT1>(tile, tw);
+  if constexpr (Op::FFT2 != 0) {
+#pragma unroll 4
+    for (int i = threadIdx.x; i < N * W; i += NT) {
+      int l, c, y, x;
+      stage_coords<N, AXIS>(i, g, l, c, y, x);
+      const int t = tidx<W>(l, c);
+      tile[t] = op.mid(tile[t], base + (size_t)y * N + x, g.p, y, x, acc);
+    }
+    __syncthreads();
+    Plan<N>::template run<W, Op::FFT2>(tile, tw);
+  }
+#pragma unroll 4
+  for (int i = threadIdx.x; i < N * W; i += NT) {
+    int l, c, y, x;
+    stage_coords<N, AXIS>(i, g, l, c, y, x);
+    op.store(tile[tidx<W>(l, c)], base + (size_t)y * N + x, g.p, y, x, acc);
+  }
+  if constexpr (Op::NSUM + Op::NMAX > 0) {
+    double v[NRED];
+    acc.values(v);
+    block_reduce_store<NT, Op::NSUM, Op::NMAX>(op.partials, v);
+  }
+  if constexpr (Op::PEAK) block_argmax_store<NT>(op.partials, acc.mx, acc.idx);
+}
+
+struct NoAcc {
+  __device__ void values(double (&v)[NRED]) const {
+#pragma unroll
+    for (int k = 0; k < NRED; ++k) v[k] = 0.0;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// ops
+// ---------------------------------------------------------------------------
+struct OpBase {
+  static constexpr int NSUM = 0, NMAX = 0, PEAK = 0;
+  int first;
+  double* partials;
+};
+
+// Source transforms of the first row pass: rho itself, rho gated by the
+// support (apply_support_er on a copy), or its modulus.
+enum { SRC_RHO = 0, SRC_GATED = 1, SRC_ABS = 2 };
+
+// row pass: load rho (optionally gated / modulus) -> FFT+ (x) -> T.
+// SRC_GATED accumulates sum |rho_s| (get_module_sum, gpu_context.cu:219-246).
+template <int SRC>
+struct OpRowsForward : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = 0;
+  static constexpr int NSUM = (SRC == SRC_GATED) ? 1 : 0, NMAX = 0;
+  const float2* rho;
+  const int* S;
+  float2* T;
+  float thi, tlo;
+  struct Acc {
+    float s = 0.f;
+    __device__ void values(double (&v)[NRED]) const {
+      v[0] = s;
+      v[1] = v[2] = v[3] = 0.0;
+    }
+  };
+  __device__ float2 load(size_t gi, int, int, int, Acc& a) const {
+    float2 v = rho[gi];
+    if (SRC == SRC_GATED) {
+      const float t = phase_out(v, thi, tlo) ? 0.f : (float)S[gi];
+      v = make_float2(v.x * t, v.y * t);
+      a.s += cabsf2(v);
+    } else if (SRC == SRC_ABS) {
+      v = make_float2(cabsf2(v), 0.f);
+    }
+    return v;
+  }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
+};
+
+// column pass: T -> FFT+ (y) -> P_M -> FFT- (y) -> T
+struct OpColsProject : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = -1, NSUM = 0, NMAX = 0;
+  float2* T;
+  const float* A;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  int n;
+  __device__ float2 mid(float2 v, size_t, int, int y, int x, Acc&) const {
+    return project(v, __ldg(A + (size_t)y * n + x));
+  }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
+};
+
+// Support updates (reference apply_support_{hio,raar,er},
+// gpu_context.cu:519-593).  rp: the projected iterate rho', prev: the
+// previous iterate (the reference's buffer, always equal to rho).
+enum { UPD_HIO = 0, UPD_RAAR = 1, UPD_ER = 2 };
+
+template <int UPD>
+__device__ __forceinline__ float2 update(float2 rp, float2 prev, int s, float beta, float thi, float tlo) {
+  if (UPD == UPD_ER) {
+    const float t = phase_out(rp, thi, tlo) ? 0.f : (float)s;
+    return make_float2(rp.x * t, rp.y * t);
+  } else if (UPD == UPD_HIO) {
+    const float t = phase_out(rp, thi, tlo) ? 0.f : (float)s;
+    const float u = 1.f - t;
+    return make_float2(fmaf(fmaf(-beta, rp.x, prev.x), u, rp.x * t),
+                       fmaf(fmaf(-beta, rp.y, prev.y), u, rp.y * t));
+  } else {
+    const float2 refl = make_float2(2.f * rp.x - prev.x, 2.f * rp.y - prev.y);
+    if (s == 0 || phase_out(refl, thi, tlo)) {
+      const float k = 1.f - 2.f * beta;
+      return make_float2(fmaf(beta, prev.x, k * rp.x), fmaf(beta, prev.y, k * rp.y));
+    }
+    return rp;
+  }
+}
+
+// row pass of an iteration: T -> FFT- (x) -> /N^2 -> update -> rho -> FFT+ (x) -> T
+template <int UPD>
+struct OpRowsIterate : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = +1, NSUM = 0, NMAX = 0;
+  float2* T;
+  float2* rho;
+  const int* S;
+  float scale, beta, thi, tlo;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t gi, int, int, int, Acc&) const {
+    const float2 rp = make_float2(v.x * scale, v.y * scale);
+    const float2 prev = (UPD == UPD_ER) ? make_float2(0.f, 0.f) : rho[gi];
+    const float2 r = update<UPD>(rp, prev, S[gi], beta, thi, tlo);
+    rho[gi] = r;
+    return r;
+  }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
+};
+
+// last row pass of a call: T -> FFT- (x) -> /N^2 -> rho (the trailing
+// modulus projection of GPU_context::HIO/RAAR/ER, gpu_context.cu:803-812)
+struct OpRowsFinal : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 0, NMAX = 0;
+  float2* T;
+  float2* out;
+  float scale;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const {
+    out[gi] = make_float2(v.x * scale, v.y * scale);
+  }
+};
+
+// ---- shrink-wrap (reference GPU_context::SW/SWA, gpu_context.cu:906-1027)
+
+// row pass: T -> FFT- (x) -> |./N^2| (get_module) -> FFT+ (x) -> T
+struct OpRowsModulusForward : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = +1, NSUM = 0, NMAX = 0;
+  float2* T;
+  float scale;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const {
+    return make_float2(cabsf2(make_float2(v.x * scale, v.y * scale)), 0.f);
+  }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
+};
+
+// column pass: T -> FFT+ (y) -> * exp(-r^2/sigma_ft^2) (smooth_intensities,
+// r measured from the corner origin) -> FFT- (y) -> T
+struct OpColsBlur : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = -1, NSUM = 0, NMAX = 0;
+  float2* T;
+  int n;
+  float sig2;  // sigma_ft^2
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int y, int x, Acc&) const {
+    const int xx = (x >= n / 2) ? x - n : x;
+    const int yy = (y >= n / 2) ? y - n : y;
+    const float r2 = (float)(xx * xx + yy * yy);
+    const float k = expf(-__fdiv_rn(r2, sig2));
+    return make_float2(v.x * k, v.y * k);
+  }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
+};
+
+// row pass: T -> FFT- (x) -> M = |.| (float), per-CTA max (get_max_module)
+struct OpRowsMagnitude : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 0, NMAX = 1;
+  const float2* T;
+  float* M;
+  struct Acc {
+    float mx = 0.f;
+    __device__ void values(double (&v)[NRED]) const {
+      v[0] = mx;
+      v[1] = v[2] = v[3] = 0.0;
+    }
+  };
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc& a) const {
+    const float m = cabsf2(v);
+    M[gi] = m;
+    a.mx = fmaxf(a.mx, m);
+  }
+};
+
+// ---- error metrics (reference GPU_context::get_error, gpu_context.cu:1030-1134)
+
+// column pass on the transform of the gated density: FFT+ (y) gives F;
+// accumulate sum_{A>=0} (A-|F|)^2, sum_{A>=0} A^2 and max |F|
+// (get_error_gpu, get_max_module); then P_M -> FFT- (y) -> T
+struct OpColsError : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = -1, NSUM = 2, NMAX = 1;
+  float2* T;
+  const float* A;
+  int n;
+  struct Acc {
+    float e = 0.f, a2 = 0.f, mx = 0.f;
+    __device__ void values(double (&v)[NRED]) const {
+      v[0] = e;
+      v[1] = a2;
+      v[2] = mx;
+      v[3] = 0.0;
+    }
+  };
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int y, int x, Acc& acc) const {
+    const float a = __ldg(A + (size_t)y * n + x);
+    const float m = cabsf2(v);
+    acc.mx = fmaxf(acc.mx, m);
+    if (a >= 0.f) {
+      acc.a2 += a * a;
+      acc.e += (a - m) * (a - m);
+    }
+    return project(v, a);
+  }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
+};
+
+// row pass: T -> FFT- (x) -> /N^2 -> real-space error terms of
+// get_real_error_gpu (gpu_context.cu:386-434), including its x*xs term
+struct OpRowsRealError : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 2, NMAX = 0;
+  const float2* T;
+  const int* S;
+  float scale, thi, tlo;
+  struct Acc {
+    float err = 0.f, nrm = 0.f;
+    __device__ void values(double (&v)[NRED]) const {
+      v[0] = err;
+      v[1] = nrm;
+      v[2] = v[3] = 0.0;
+    }
+  };
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc& a) const {
+    const float2 r = make_float2(v.x * scale, v.y * scale);
+    const int s = S[gi];
+    const float t = phase_out(r, thi, tlo) ? 0.f : (float)s;
+    const float xs = r.x * t, ys = r.y * t;
+    a.nrm += r.y * r.y + r.x * r.x;
+    if (s == 0) a.err += (r.y - ys) * (r.y - ys) + (r.x * xs) * (r.x * xs);
+  }
+};
+
+// ---- cross-correlations (get_symmetry / get_shift, gpu_context.cu:1157-1463)
+
+// column pass: T -> FFT+ (y) -> T (finishes D = FFT(|rho|))
+struct OpColsForward : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = 0, NSUM = 0, NMAX = 0;
+  const float2* src;
+  float2* dst;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return src[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { dst[gi] = v; }
+};
+
+// Band-pass weight of multiply() (gpu_context.cu:1157-1200), squared.
+__device__ __forceinline__ float bandpass2(int x, int y, int n, float minr, float maxr) {
+  const float fx = (float)((x >= n / 2) ? x - n : x);
+  const float fy = (float)((y >= n / 2) ? y - n : y);
+  const float radius = sqrtf(fx * fx + fy * fy);
+  const float sigtot = (float)((double)n * (double)minr / 2. + 1e-12);
+  const float sig = (float)((double)sigtot / 10.);
+  const float eff = radius - (sigtot - sig);
+  float coeff = eff > 0.f ? 1.f - expf(-__fdiv_rn(eff * eff, sig * sig)) : 0.f;
+  const float sigtotm = (float)((double)n * (double)maxr / 2. + 1e-12);
+  const float sigm = (float)((double)sigtotm / 10.);
+  const float effm = radius - (sigtotm - sigm);
+  const float coeffm = effm > 0.f ? expf(-__fdiv_rn(effm * effm, sigm * sigm)) : 1.f;
+  coeff *= coeffm;
+  return coeff * coeff;
+}
+
+// normalize_ft_shift with exponent 1 (gpu_context.cu:37-50): identity, NaN
+// where |D| == 0.
+__device__ __forceinline__ float2 ft_shift_norm(float2 d) {
+  const float m = cabsf2(d);
+  if (m == 0.f) {
+    const float q = __int_as_float(0x7fffffff);
+    return make_float2(q, q);
+  }
+  return d;
+}
+
+// column pass: form the band-passed cross-power spectrum of D (individual
+// spectrum) with Dref (reference spectrum, one per individual or shared),
+// conj(D) Dref (SIGN=-1) or D Dref (SIGN=+1), masked where A < 0; then
+// FFT- (y) -> dst.
+template <int SIGN>
+struct OpColsCrossPower : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 0, NMAX = 0;
+  const float2* D;
+  const float2* Dref;
+  size_t ref_stride;  // elements between references of consecutive individuals (0: shared)
+  int ref_first;
+  float2* dst;
+  const float* A;
+  int n;
+  float minr, maxr;
+  int norm_d, norm_ref;  // apply normalize_ft_shift
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int p, int y, int x, Acc&) const {
+    float2 d = D[gi];
+    const size_t pix = (size_t)y * n + x;
+    float2 r = Dref[(size_t)(p - first + ref_first) * ref_stride + pix];
+    if (norm_d) d = ft_shift_norm(d);
+    if (norm_ref) r = ft_shift_norm(r);
+    const float sd = (float)SIGN * d.y;
+    float2 c = make_float2(d.x * r.x - sd * r.y, d.x * r.y + sd * r.x);
+    const float w = bandpass2(x, y, n, minr, maxr);
+    c = make_float2(c.x * w, c.y * w);
+    if (__ldg(A + pix) < 0.f) c = make_float2(0.f, 0.f);
+    return c;
+  }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { dst[gi] = v; }
+};
+
+// row pass: T -> FFT- (x) -> |.|^2; per-CTA max and the raster index of its
+// first occurrence (encoded as a double-precision pair: value, index)
+struct OpRowsPeak : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 0, NMAX = 0, PEAK = 1;
+  const float2* T;
+  int n;
+  struct Acc {
+    float mx = 0.f;
+    int idx = 0x7fffffff;
+    __device__ void values(double (&v)[NRED]) const {
+      v[0] = v[1] = v[2] = v[3] = 0.0;
+    }
+  };
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t, int, int y, int x, Acc& a) const {
+    const float val = v.x * v.x + v.y * v.y;
+    const int i = y * n + x;
+    // strict '>' in raster order keeps the first maximum; NaN never wins
+    if (val > a.mx || (val == a.mx && val > 0.f && i < a.idx)) {
+      a.mx = val;
+      a.idx = i;
+    }
+  }
+};
+
+}  // namespace spe

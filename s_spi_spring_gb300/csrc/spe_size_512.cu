@@ -1,0 +1,3 @@
+// Instantiates the fused pass kernels for pattern side(s): 512.
+#include "spe_sizes.cuh"
+SPE_DEFINE_SIZE(512)

@@ -1,0 +1,3 @@
+// Instantiates the fused pass kernels for pattern side(s): 768.
+#include "spe_sizes.cuh"
+SPE_DEFINE_SIZE(768)

@@ -1,0 +1,246 @@
+"""GPU parity of the engine against the CPU oracle, through the C ABI.
+
+Tolerances (float32 engine vs float64 oracle, relative L2 over each
+individual): one projection / one iteration 2e-6; 20 ER iterations 2e-5.
+HIO and RAAR amplify rounding differences from a random start (their
+out-of-support update is expansive), so 20 iterations from a random start are
+compared at 5e-3 and through the R-factor trajectory (1e-3 relative), and 20
+iterations started next to the solution at 2e-5.  Metrics: 1e-5 relative
+(R-factor, sums), 1e-4 (real-space error, symmetry).  Supports from
+shrink-wrap must match exactly except at pixels whose blurred modulus lies
+within 1e-4 (relative) of the threshold.
+"""
+import numpy as np
+import pytest
+
+from oracle import spring_oracle as o
+from s_spi_spring_gb300 import _lib, synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-30))
+
+
+def setup_case(n, count, seed=0, photons=1e7):
+    if n >= 256:
+        I, obj, supp = synthetic.polygon_pattern(seed=seed, n=n, diameter=n * 0.23, photons=photons,
+                                                 stop_radius=max(2, n // 64))
+    else:
+        I, obj, supp = synthetic.disc_pattern(seed=seed, n=n, radius=n * 0.16, photons=photons,
+                                              beamstop=max(1, n // 32) | 1)
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    dens, S = synthetic.start_population(n, count, n * 0.2, seed=seed + 100)
+    return A, dens, S
+
+
+def make_engine(n, A, dens, S):
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, dens, S)
+    return e
+
+
+@pytest.mark.parametrize("n", [16, 64, 128, 256, 384, 512, 768, 1024, 2048])
+def test_transform_round_trip_identity(n):
+    """All pixels unknown: P_M is the identity, so ER(0) = F^-1 F rho."""
+    A = -np.ones((n, n), np.float32)
+    rng = np.random.default_rng(n)
+    dens = (rng.standard_normal((2, n, n)) + 1j * rng.standard_normal((2, n, n))).astype(np.complex64)
+    S = np.ones((2, n, n), np.int32)
+    e = make_engine(n, A, dens, S)
+    e.er(0, 2, 0)
+    got, s2 = e.download(0, 2)
+    assert np.array_equal(s2, S)
+    for i in range(2):
+        assert rel(got[i], dens[i]) < 2e-6
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 384, 512, 768, 1024])
+def test_projection_matches_oracle(n):
+    A, dens, S = setup_case(n, 2, seed=n)
+    e = make_engine(n, A, dens, S)
+    e.hio(0, 2, 0, 0.9, 0.0)  # zero iterations: only the trailing projection
+    got, _ = e.download(0, 2)
+    for i in range(2):
+        ref = o.modulus_projection(dens[i].astype(complex), A)
+        assert rel(got[i], ref) < 2e-6, (n, i, rel(got[i], ref))
+
+
+ALGS = [("HIO", 0.9), ("RAAR", 0.87), ("ER", 0.0)]
+
+
+@pytest.mark.parametrize("n", [64, 128, 384, 512])
+@pytest.mark.parametrize("alg,beta", ALGS)
+@pytest.mark.parametrize("reality", [0.0, 0.5])
+def test_iterations_match_oracle(n, alg, beta, reality):
+    A, dens, S = setup_case(n, 3, seed=n + 7)
+    e = make_engine(n, A, dens, S)
+    for iters, tol in ((1, 2e-6), (20, 2e-5 if alg == "ER" else 5e-3)):
+        e.upload(0, dens, S)
+        if alg == "HIO":
+            e.hio(0, 3, iters, beta, reality)
+        elif alg == "RAAR":
+            e.raar(0, 3, iters, beta, reality)
+        else:
+            e.er(0, 3, iters, reality)
+        got, gs = e.download(0, 3)
+        assert np.array_equal(gs, S)
+        for i in range(3):
+            d = dens[i].astype(complex)
+            if alg == "HIO":
+                ref = o.hio(d, S[i], A, iters, beta, reality)
+            elif alg == "RAAR":
+                ref = o.raar(d, S[i], A, iters, beta, reality)
+            else:
+                ref = o.er(d, S[i], A, iters, reality)
+            r = rel(got[i], ref)
+            print(f"{alg} n={n} it={iters} real={reality} ind={i} rel={r:.2e}")
+            assert r < tol, (alg, n, iters, i, r)
+
+
+@pytest.mark.parametrize("alg,beta", ALGS)
+def test_iterations_near_solution_match_oracle(alg, beta):
+    """Started next to the true object, all three algorithms stay close to the
+    oracle for many iterations."""
+    n = 256
+    I, obj, supp = synthetic.polygon_pattern(seed=5, n=n, diameter=60, photons=1e9, stop_radius=3)
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    rng = np.random.default_rng(6)
+    start = (obj * (1 + 0.01 * rng.standard_normal(obj.shape))).astype(np.complex64)[None]
+    S = supp[None].astype(np.int32)
+    e = make_engine(n, A, start, S)
+    getattr(e, alg.lower())(0, 1, 20, *(() if alg == "ER" else (beta,)), 0.0)
+    got, _ = e.download(0, 1)
+    f = {"HIO": o.hio, "RAAR": o.raar}.get(alg)
+    ref = o.er(start[0].astype(complex), S[0], A, 20, 0.0) if f is None else f(start[0].astype(complex), S[0], A, 20, beta, 0.0)
+    r = rel(got[0], ref)
+    print(alg, "near-solution rel", r)
+    assert r < 2e-5
+
+
+@pytest.mark.parametrize("alg,beta", [("HIO", 0.9), ("RAAR", 0.87)])
+def test_rfactor_trajectory_matches_oracle(alg, beta):
+    """R-factor after every 5 iterations over 40 iterations from a random start."""
+    n = 128
+    A, dens, S = setup_case(n, 2, seed=21)
+    e = make_engine(n, A, dens, S)
+    cur = [dens[i].astype(complex) for i in range(2)]
+    for step in range(8):
+        getattr(e, alg.lower())(0, 2, 5, beta, 0.0)
+        ms = e.evaluate(0, 2, 0.0, 0.0)
+        for i in range(2):
+            cur[i] = getattr(o, alg.lower())(cur[i], S[i], A, 5, beta, 0.0)
+            ref = o.get_error(cur[i], S[i], A, 0.0).error_fourier
+            print(alg, step, i, ms[i]["error_fourier"], ref)
+            assert abs(ms[i]["error_fourier"] - ref) <= 1e-3 * ref
+
+
+def test_subset_range_leaves_others_untouched():
+    n = 128
+    A, dens, S = setup_case(n, 5, seed=3)
+    e = make_engine(n, A, dens, S)
+    e.raar(1, 2, 5, 0.87, 0.0)
+    got, _ = e.download(0, 5)
+    for i in (0, 3, 4):
+        assert np.array_equal(got[i], dens[i])
+    for i in (1, 2):
+        ref = o.raar(dens[i].astype(complex), S[i], A, 5, 0.87, 0.0)
+        assert rel(got[i], ref) < 2e-5
+
+
+def _support_agrees(got, ref_S, m, thr):
+    diff = got != ref_S
+    if not diff.any():
+        return True
+    near = np.abs(m - thr) <= 1e-4 * max(thr, 1e-30)
+    return bool(np.all(near[diff]))
+
+
+@pytest.mark.parametrize("n", [64, 256, 512])
+def test_shrinkwrap_matches_oracle(n):
+    A, dens, S = setup_case(n, 2, seed=n + 1)
+    e = make_engine(n, A, dens, S)
+    # run a few ER iterations so the densities are object-like
+    e.er(0, 2, 5, 0.0)
+    base, _ = e.download(0, 2)
+    for sigma, thr in ((3.0, 0.1), (1.5, 0.05)):
+        e.upload(0, base, S)
+        e.sw(0, 2, sigma, thr, 0.0)
+        gd, gs = e.download(0, 2)
+        assert np.array_equal(gd, base)  # density restored
+        for i in range(2):
+            m = o.blurred_modulus(base[i].astype(complex), A, sigma)
+            ref = o.sw(base[i].astype(complex), S[i], A, sigma, thr)
+            assert _support_agrees(gs[i], ref, m, m.max() * np.float32(thr)), (n, sigma, i)
+    for sigma, k in ((2.5, 500), (1.0, 2000), (2.0, 1)):
+        e.upload(0, base, S)
+        e.swa(0, 2, sigma, k, 0.0)
+        gd, gs = e.download(0, 2)
+        for i in range(2):
+            m = o.blurred_modulus(base[i].astype(complex), A, sigma)
+            t = o.swa_threshold(m, k)
+            ref = (m >= t).astype(np.int32)
+            assert _support_agrees(gs[i], ref, m, t), (n, sigma, k, i)
+            assert gs[i].sum() >= min(k, int((m >= t).sum()) - 2)
+
+
+@pytest.mark.parametrize("n", [64, 256, 512])
+@pytest.mark.parametrize("reality", [0.0, 0.5])
+def test_evaluate_matches_oracle(n, reality):
+    A, dens, S = setup_case(n, 3, seed=n + 2)
+    e = make_engine(n, A, dens, S)
+    e.hio(0, 3, 10, 0.9, reality)
+    cur, _ = e.download(0, 3)
+    ms = e.evaluate(0, 3, reality, 0.25)
+    for i in range(3):
+        ref = o.evaluate(cur[i].astype(complex), S[i], A, reality, 0.25)
+        print(n, reality, i, {k: (ms[i][k], ref[k]) for k in ref})
+        for k, tol in (("error_fourier", 1e-5), ("modulesum", 1e-5), ("complexsum", 1e-5),
+                       ("error", 1e-5), ("error_real", 1e-4), ("symmetry", 1e-4)):
+            assert abs(ms[i][k] - ref[k]) <= tol * abs(ref[k]) + 1e-7, (k, ms[i][k], ref[k])
+
+
+def test_sequence_equals_individual_calls():
+    n = 128
+    A, dens, S = setup_case(n, 4, seed=9)
+    ops = [_lib.SpeOp(_lib.SPE_OP_HIO, 8, 0.9, 0, 0, 0), _lib.SpeOp(_lib.SPE_OP_ER, 4, 0, 0, 0, 0),
+           _lib.SpeOp(_lib.SPE_OP_SW, 0, 0, 2.0, 0.05, 0), _lib.SpeOp(_lib.SPE_OP_SWA, 0, 0, 1.5, 0, 300)]
+    e1 = make_engine(n, A, dens, S)
+    m1 = e1.sequence(0, 4, ops, nrep=2, reality=0.0)
+    d1, s1 = e1.download(0, 4)
+    e2 = make_engine(n, A, dens, S)
+    for _ in range(2):
+        e2.hio(0, 4, 8, 0.9, 0.0)
+        e2.er(0, 4, 4, 0.0)
+        e2.sw(0, 4, 2.0, 0.05, 0.0)
+        e2.swa(0, 4, 1.5, 300, 0.0)
+    m2 = e2.evaluate(0, 4, 0.0, 0.0)
+    d2, s2 = e2.download(0, 4)
+    assert np.array_equal(d1, d2) and np.array_equal(s1, s2)
+    assert m1 == m2
+
+
+def test_solver_api_single_and_list():
+    from s_spi_spring_gb300.spring_core.phase_retrieval import Reconstruction, Solver
+    n = 64
+    I, _, _ = synthetic.disc_pattern(seed=11, n=n, radius=10)
+    dens, S = synthetic.start_population(n, 3, 12, seed=12)
+    sol = Solver(I, gpus=[0])
+    recs = [Reconstruction(dens[i], S[i]) for i in range(3)]
+    single = Reconstruction(dens[1], S[1])
+    out = sol.HIO(recs, 5, 0.9)
+    assert out is not None and len(out) == 3 and out[0] is recs[0]
+    r1 = sol.HIO(single, 5, 0.9)
+    assert r1 is single
+    assert np.array_equal(recs[1].get_density(), single.get_density())
+    A = sol.get_pattern()
+    ref = o.hio(dens[1].astype(complex), S[1], A, 5, 0.9, 0.0)
+    assert rel(single.get_density(), ref) < 1e-5
+    sol.set_sequence([("HIO", [5, 0.9]), ("ER", [5]), ("SW", [2.0, 0.05]), ("BAD", [1])])
+    sol.Sequence(recs)
+    for r in recs:
+        assert 0 < r.get_error() < 1 and r.get_symmetry() > 0
+    sol.Evaluate(single)
+    assert single.get_error() > 0
