@@ -148,6 +148,54 @@ int spe_evaluate(spe_engine* e, int first, int count, float reality, float realp
 int spe_sequence(spe_engine* e, int first, int count, const spe_op* ops, int nops, int nrep, float reality,
                  float realpen, spe_metrics* metrics);
 
+/* ---- population-level operations (slots are population indices) ---- */
+
+/* Seeds the random generator that steers the crossover draws: the
+ * generator of the reference's first context, std::mt19937 seeded with
+ * (0+1)*seed (src/solver.cpp:37, src/context.h:13). */
+int spe_seed(spe_engine* e, uint32_t seed);
+
+/* Solver::Reshift (src/solver.cpp:511-538) with GPU_context::set_ref_density,
+ * get_shift and reshift (gpu_context.cu:632-667, 1226-1371): aligns each
+ * individual of [first, first+count) to the reference (translation, global
+ * phase, twin flip) by the band-passed cross-correlation of the modulus
+ * spectra (radii minr..maxr).  The reference is population slot ref_slot,
+ * or, when ref_slot < 0, the host density ref_density (n*n complex64). */
+int spe_reshift(spe_engine* e, int first, int count, int ref_slot, const float* ref_density, float minr,
+                float maxr);
+
+/* Solver::GetAverage (src/solver.cpp:618-686): mean density and OR-ed
+ * support of the int(fraction*count) individuals with the lowest errors
+ * (errors: count floats), written to population slot out_slot. */
+int spe_average(spe_engine* e, int first, int count, const float* errors, float fraction, int out_slot);
+
+/* Solver::GetAverageModule (src/solver.cpp:564-614): mean of |FFT(rho)| (ft
+ * != 0) or |rho| over the best int(fraction*count) individuals; kept on the
+ * device for the crossover and copied to `out` (n*n floats) when not NULL. */
+int spe_average_module(spe_engine* e, int first, int count, const float* errors, int ft, float fraction,
+                       float* out);
+
+/* Solver::Crossover (src/solver.cpp:716-817) with GPU_context::
+ * prepare_parents and get_new_individual (gpu_context.cu:1468-1694,
+ * 1699-1883, 2044-2117): one child per individual of [first, first+count)
+ * into [dst_first, dst_first+count).  best_slot and avg_slot hold the best
+ * and the average reconstruction.  Random draws follow the reference's
+ * single-context order from the engine's generator (spe_seed).  The
+ * children's error fields are the parents' (the reference copies them). */
+int spe_crossover(spe_engine* e, int first, int count, const float* errors, int best_slot, int avg_slot,
+                  int dst_first, float crossbalance, float crossdiff, float crossexp, float crossft, int crosssym,
+                  float use_average, int update_support, float reality, float minr, float maxr);
+
+/* Host-only: the random draws of Solver::Crossover (src/solver.cpp:750-801)
+ * for `count` children from std::mt19937(seed), given the error order and
+ * suppdim.  draws: count*11 ints (p1, p2, p3, crossft, squaresizex,
+ * squaresizey, crosssizex, crosssizey, offsetx, offsety, crossmap offset);
+ * rot: count floats; cmaps (may be NULL to query cmaps_used): the crossmaps
+ * concatenated.  No device is touched. */
+int spe_crossover_draws(uint32_t seed, int count, const int32_t* order, float suppdim, int n, float crossbalance,
+                        float crossexp, float crossft, int32_t* draws, float* rot, int32_t* cmaps, int cmaps_capacity,
+                        int32_t* cmaps_used);
+
 /* Waits for all work queued on the engine's stream. */
 int spe_synchronize(spe_engine* e);
 

@@ -61,6 +61,12 @@ SIGNATURES = {
     "spe_evaluate": (_i, [_vp, _i, _i, _f, _f, C.POINTER(SpeMetrics)]),
     "spe_sequence": (_i, [_vp, _i, _i, C.POINTER(SpeOp), _i, _i, _f, _f, C.POINTER(SpeMetrics)]),
     "spe_synchronize": (_i, [_vp]),
+    "spe_seed": (_i, [_vp, C.c_uint32]),
+    "spe_reshift": (_i, [_vp, _i, _i, _i, _fp, _f, _f]),
+    "spe_average": (_i, [_vp, _i, _i, _fp, _f, _i]),
+    "spe_average_module": (_i, [_vp, _i, _i, _fp, _i, _f, _fp]),
+    "spe_crossover": (_i, [_vp, _i, _i, _fp, _i, _i, _i, _f, _f, _f, _f, _i, _f, _i, _f, _f, _f]),
+    "spe_crossover_draws": (_i, [C.c_uint32, _i, _ip, _f, _i, _f, _f, _f, _ip, _fp, _ip, _i, _ip]),
 }
 
 
@@ -207,9 +213,52 @@ class Engine:
     def synchronize(self):
         call("spe_synchronize", self.h)
 
+    # -- population-level operations --------------------------------------------
+    def seed(self, seed: int):
+        call("spe_seed", self.h, C.c_uint32(int(seed) & 0xFFFFFFFF))
+
+    def reshift(self, first, count, ref_slot=-1, ref_density=None, minr=0.0, maxr=2.0):
+        r = None if ref_density is None else np.ascontiguousarray(ref_density, dtype=np.complex64)
+        call("spe_reshift", self.h, int(first), int(count), int(ref_slot),
+             None if r is None else r.view(np.float32).ctypes.data_as(_fp), float(minr), float(maxr))
+
+    def average(self, first, count, errors, fraction, out_slot):
+        err = np.ascontiguousarray(errors, dtype=np.float32)
+        call("spe_average", self.h, int(first), int(count), fptr(err), float(fraction), int(out_slot))
+
+    def average_module(self, first, count, errors, ft=True, fraction=1.0):
+        err = np.ascontiguousarray(errors, dtype=np.float32)
+        out = np.empty((self.n, self.n), np.float32)
+        call("spe_average_module", self.h, int(first), int(count), fptr(err), int(bool(ft)), float(fraction), fptr(out))
+        return out
+
+    def crossover(self, first, count, errors, best_slot, avg_slot, dst_first, crossbalance, crossdiff,
+                  crossexp=1.0, crossft=1.0, crosssym=False, use_average=0.0, update_support=True,
+                  reality=0.0, minr=0.0, maxr=2.0):
+        err = np.ascontiguousarray(errors, dtype=np.float32)
+        call("spe_crossover", self.h, int(first), int(count), fptr(err), int(best_slot), int(avg_slot),
+             int(dst_first), float(crossbalance), float(crossdiff), float(crossexp), float(crossft),
+             int(bool(crosssym)), float(use_average), int(bool(update_support)), float(reality),
+             float(minr), float(maxr))
+
 
 def metrics_dict(m: SpeMetrics) -> dict:
     return {k: float(getattr(m, k)) for k, _ in SpeMetrics._fields_}
+
+
+def crossover_draws(seed, order, suppdim, n, crossbalance, crossexp=1.0, crossft=1.0):
+    """Host-only draws of the crossover (see include/spe_engine.h)."""
+    order = np.ascontiguousarray(order, dtype=np.int32)
+    count = len(order)
+    draws = np.empty((count, 11), np.int32)
+    rot = np.empty(count, np.float32)
+    used = C.c_int32()
+    args = [C.c_uint32(int(seed) & 0xFFFFFFFF), count, iptr(order), float(suppdim), int(n), float(crossbalance),
+            float(crossexp), float(crossft), iptr(draws), fptr(rot)]
+    call("spe_crossover_draws", *args, None, 0, C.byref(used))
+    cm = np.empty(max(used.value, 1), np.int32)
+    call("spe_crossover_draws", *args, iptr(cm), cm.size, C.byref(used))
+    return draws, rot, cm[:used.value]
 
 
 def prepare_pattern(intensities, center=(-1, -1), use_bounds=True):

@@ -9,6 +9,7 @@
 
 #include "../../include/spe_engine.h"
 #include "spe_internal.h"
+#include "spe_engine_impl.h"
 
 namespace spe {
 const SizeOps* size_ops_16();
@@ -150,33 +151,7 @@ __global__ void k_select_pick(uint32_t* __restrict__ state, uint32_t* __restrict
 
 }  // namespace spe
 
-// ---------------------------------------------------------------------------
-// engine
-// ---------------------------------------------------------------------------
-struct spe_engine {
-  int dev = 0;
-  int n = 0;
-  size_t npix = 0;
-  const spe::SizeOps* ops = nullptr;
-  cudaStream_t own = nullptr;
-  cudaStream_t st = nullptr;
-  int cap = 0;
-  bool have_amp = false;
-  float* A = nullptr;
-  float2* tw = nullptr;
-  float2* rho = nullptr;
-  int* S = nullptr;
-  float2* T = nullptr;
-  float2* T2 = nullptr;
-  float* M = nullptr;
-  double* partials = nullptr;  // 5 regions of cap * tpi * NRED
-  double* red = nullptr;       // cap * 16
-  double* red_host = nullptr;  // pinned
-  uint32_t* sel_state = nullptr;
-  uint32_t* sel_hist = nullptr;
-};
-
-namespace {
+namespace spe_detail {
 
 thread_local std::string g_err;
 
@@ -193,12 +168,6 @@ int fail(int code, const char* fmt, ...) {
 int cuda_fail(cudaError_t e, const char* what) {
   return fail(e == cudaErrorMemoryAllocation ? SPE_ERR_NOMEM : SPE_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
-
-#define CK(call, what)                             \
-  do {                                             \
-    cudaError_t e_ = (call);                       \
-    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-  } while (0)
 
 float largest_float_not_above(double t) {
   float f = (float)t;
@@ -250,17 +219,18 @@ spe::Ctx make_ctx(spe_engine* e, int first, int count) {
   return c;
 }
 
-size_t region(spe_engine* e) { return (size_t)e->cap * e->ops->tiles_per_individual * spe::NRED; }
+size_t max_tiles(const spe::SizeOps* o) { return (size_t)std::max(o->tiles_rows, o->tiles_cols); }
+size_t region(spe_engine* e) { return (size_t)e->cap * max_tiles(e->ops) * spe::NRED; }
 
-int reduce(spe_engine* e, const double* part, int count, int k, int is_max, int slot) {
-  const int tpi = e->ops->tiles_per_individual;
+// tpi: CTAs per individual of the pass that wrote the partials
+int reduce(spe_engine* e, const double* part, int count, int tpi, int k, int is_max, int slot) {
   spe::k_reduce<<<(count + 127) / 128, 128, 0, e->st>>>(part, count, tpi, k, is_max, e->red, 16, slot);
   CK(cudaGetLastError(), "reduce launch");
   return SPE_OK;
 }
 
 int reduce_peak(spe_engine* e, const double* part, int count, int slot) {
-  const int tpi = e->ops->tiles_per_individual;
+  const int tpi = e->ops->tiles_rows;
   spe::k_reduce_peak<<<(count + 127) / 128, 128, 0, e->st>>>(part, count, tpi, e->red, 16, slot);
   CK(cudaGetLastError(), "peak reduce launch");
   return SPE_OK;
@@ -317,7 +287,7 @@ int do_shrinkwrap(spe_engine* e, int first, int count, float sigma, bool absolut
   CK(e->ops->blur_magnitude(c, sft), "shrink-wrap kernels");
   const unsigned grid = 152 * 8;
   if (!absolute) {
-    if ((rc = reduce(e, e->partials, count, 0, 1, 0))) return rc;
+    if ((rc = reduce(e, e->partials, count, e->ops->tiles_rows, 0, 1, 0))) return rc;
     spe::k_threshold_rel<<<grid, 256, 0, e->st>>>(e->M, e->S, e->red, 16, threshold, e->npix, first, count);
     CK(cudaGetLastError(), "threshold launch");
     return SPE_OK;
@@ -341,7 +311,9 @@ int do_shrinkwrap(spe_engine* e, int first, int count, float sigma, bool absolut
   return SPE_OK;
 }
 
-}  // namespace
+}  // namespace spe_detail
+
+using namespace spe_detail;
 
 extern "C" {
 
@@ -378,14 +350,11 @@ int spe_create(int n, int device, spe_engine** out) {
     return cuda_fail(err, "stream");
   }
   e->st = e->own;
-  std::vector<float2> tw(n);
-  for (int m = 0; m < n; ++m) {
-    const double a = 2.0 * M_PI * (double)m / (double)n;
-    tw[m] = make_float2((float)std::cos(a), (float)std::sin(a));
-  }
-  err = cudaMalloc(&e->tw, n * sizeof(float2));
+  std::vector<float2> tw(ops->tw_size);
+  ops->fill_tw(tw.data());
+  err = cudaMalloc(&e->tw, tw.size() * sizeof(float2));
   if (err == cudaSuccess) err = cudaMalloc(&e->A, e->npix * sizeof(float));
-  if (err == cudaSuccess) err = cudaMemcpy(e->tw, tw.data(), n * sizeof(float2), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(e->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
   if (err != cudaSuccess) {
     cudaFree(e->tw);
     cudaFree(e->A);
@@ -404,6 +373,9 @@ int spe_destroy(spe_engine* e) {
   free_population(e);
   cudaFree(e->A);
   cudaFree(e->tw);
+  cudaFree(e->avg_mod);
+  cudaFree(e->ref);
+  cudaFree(e->work);
   cudaStreamDestroy(e->own);
   delete e;
   return SPE_OK;
@@ -449,7 +421,7 @@ int spe_reserve(spe_engine* e, int capacity) {
   spe_engine t = *e;  // new buffers
   t.cap = capacity;
   const size_t np = (size_t)capacity * e->npix;
-  const size_t tpi = e->ops->tiles_per_individual;
+  const size_t tpi = max_tiles(e->ops);
   cudaError_t err = cudaSuccess;
   t.rho = nullptr;
   t.S = nullptr;
@@ -565,12 +537,13 @@ int spe_evaluate(spe_engine* e, int first, int count, float reality, float realp
   CK(e->ops->error_terms(c, gate_er(reality), p1, p2, p3), "error kernels");
   // red slots: 0 modulesum, 1 err_f, 2 norm_f, 3 max|F|, 4 err_r, 5 norm_r,
   //            6/7 peak1 (value, index), 8/9 peak2
-  if ((rc = reduce(e, p1, count, 0, 0, 0))) return rc;
-  if ((rc = reduce(e, p2, count, 0, 0, 1))) return rc;
-  if ((rc = reduce(e, p2, count, 1, 0, 2))) return rc;
-  if ((rc = reduce(e, p2, count, 2, 1, 3))) return rc;
-  if ((rc = reduce(e, p3, count, 0, 0, 4))) return rc;
-  if ((rc = reduce(e, p3, count, 1, 0, 5))) return rc;
+  const int tr = e->ops->tiles_rows, tc = e->ops->tiles_cols;
+  if ((rc = reduce(e, p1, count, tr, 0, 0, 0))) return rc;
+  if ((rc = reduce(e, p2, count, tc, 0, 0, 1))) return rc;
+  if ((rc = reduce(e, p2, count, tc, 1, 0, 2))) return rc;
+  if ((rc = reduce(e, p2, count, tc, 2, 1, 3))) return rc;
+  if ((rc = reduce(e, p3, count, tr, 0, 0, 4))) return rc;
+  if ((rc = reduce(e, p3, count, tr, 1, 0, 5))) return rc;
   // get_symmetry (gpu_context.cu:1378-1463): D = FFT+(|rho|) normalised,
   // peaks of |FFT-(conj(D) D w)|^2 and |FFT-(D D w)|^2, band 0..1
   CK(e->ops->abs_spectrum(c, e->T2), "symmetry spectrum");

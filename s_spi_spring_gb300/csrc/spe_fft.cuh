@@ -1,32 +1,42 @@
-// Shared-memory FFT building blocks for the SPRING phase-retrieval engine.
+// Register-resident FFT building blocks for the SPRING phase-retrieval engine.
 //
-// A "tile" holds W independent complex64 transforms of length L in shared
-// memory: element (l, c) -- position l along the transform, transform c --
-// lives at  l*W + (c ^ (l & (W-1))).  The XOR swizzle makes three access
-// patterns bank-conflict free with 8-byte accesses:
-//   * W consecutive c at one l          (column staging, butterfly loads),
-//   * W consecutive l at one c          (row staging from global memory),
-//   * butterfly stores of the Stockham passes (W consecutive c per row).
+// A CTA transforms W independent complex64 sequences of length L.  Every
+// thread keeps E = L/TPT elements of one sequence in registers; shared memory
+// is used only to exchange elements between radix passes.
 //
 // The transform is the self-sorting Stockham formulation (Govindaraju et
 // al., "High performance discrete Fourier transforms on graphics
 // processors", SC'08): for a pass of radix R after passes whose radices
 // multiply to NS, butterfly b reads x[b + r*L/R], multiplies by the twiddle
 // w_{NS*R}^{(b mod NS)*r}, runs a radix-R DFT, and writes
-// x[(b/NS)*NS*R + (b mod NS) + q*NS].  Output is in natural order.
+// x[(b/NS)*NS*R + (b mod NS) + q*NS].  Output is in natural order.  Thread j
+// of a sequence runs butterflies b = j + TPT*u.  When the first and last
+// radices are equal, a thread's inputs of the first pass and its outputs of
+// the last pass sit at the same positions  b + r*L/R,  so a pointwise
+// operation between two transforms needs no data movement at all.
 //
-// Sign convention: SIGN=+1 computes sum_n x[n] exp(+2 pi i n k / L)
-// (cuFFT CUFFT_INVERSE, the reference's get_ft), SIGN=-1 the opposite
-// exponent (CUFFT_FORWARD, the reference's get_ift before /N^2).
+// Two shared-memory layouts for the exchanges, each conflict free for its
+// thread mapping (8-byte accesses):
+//   * Swz (column passes): element (l, c) at l*W + (c ^ (l & (W-1))), thread
+//     t -> c = t % W, j = t / W.  A warp covers W sequences at the same
+//     positions, so global accesses hit whole row segments of W elements.
+//   * Pad (row passes): element (l, c) at c*(L + L/16) + l + l/16, thread
+//     t -> j = t % TPT, c = t / TPT.  A warp covers 32 consecutive positions
+//     of one sequence, so global accesses are whole 256-byte row segments.
+//
+// Sign convention: S=+1 computes sum_n x[n] exp(+2 pi i n k / L) (cuFFT
+// CUFFT_INVERSE, the reference's get_ft), S=-1 the opposite exponent
+// (CUFFT_FORWARD, the reference's get_ift before /N^2).
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 namespace spe {
 
 // ---------------------------------------------------------------------------
-// compile-time trigonometry (Taylor series in double after reduction to
-// [-pi, pi]); used only to form the constant twiddles of the small DFTs.
+// compile-time trigonometry (Taylor series in double after exact reduction on
+// the integer numerator); forms the constant twiddles of the small DFTs.
 // ---------------------------------------------------------------------------
 constexpr double kPi = 3.14159265358979323846264338327950288;
 
@@ -46,7 +56,6 @@ __host__ __device__ constexpr double ct_cos_series(double x) {
   }
   return sum;
 }
-// exp(2 pi i m / R) for integers m, R, reduced exactly on the integer m.
 __host__ __device__ constexpr double ct_cos_frac(int m, int R) {
   int mm = ((m % R) + R) % R;
   if (2 * mm > R) mm -= R;  // angle in (-pi, pi]
@@ -66,14 +75,13 @@ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
-// a * (s*i), s = +-1
 template <int S>
-__device__ __forceinline__ float2 cmul_i(float2 a) {
+__device__ __forceinline__ float2 cmul_i(float2 a) {  // a * (S i)
   return S > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// multiply by the constant exp(S * 2 pi i m / R), with the trivial angles
-// (multiples of pi/2) done without multiplications.
+// multiply by the constant exp(S 2 pi i M / R); multiples of pi/2 without
+// multiplications, odd multiples of pi/4 with two.
 template <int S, int M, int R>
 __device__ __forceinline__ float2 ctwiddle(float2 a) {
   constexpr int m = ((M % R) + R) % R;
@@ -86,11 +94,9 @@ __device__ __forceinline__ float2 ctwiddle(float2 a) {
   } else if constexpr (4 * m == 3 * R) {
     return cmul_i<-S>(a);
   } else if constexpr (8 * m == R || 8 * m == 3 * R || 8 * m == 5 * R || 8 * m == 7 * R) {
-    // (+-1 +- i)/sqrt(2): two multiplications instead of four
     constexpr float h = 0.70710678118654752440f;
-    constexpr float c = float(ct_cos_frac(M, R)) > 0 ? h : -h;
-    constexpr float s = float(S * ct_sin_frac(M, R)) > 0 ? h : -h;
-    // (a.x + i a.y)(c + i s)
+    constexpr float c = ct_cos_frac(M, R) > 0 ? h : -h;
+    constexpr float s = S * ct_sin_frac(M, R) > 0 ? h : -h;
     return make_float2(c * a.x - s * a.y, c * a.y + s * a.x);
   } else {
     constexpr float c = float(ct_cos_frac(M, R));
@@ -107,8 +113,6 @@ struct SmallestFactor {
   static constexpr int value = (R % 4 == 0 && R > 4) ? 4 : (R % 2 == 0 ? 2 : (R % 3 == 0 ? 3 : R));
 };
 
-// applies y[n2*R1+k1] *= w_R^{n2*k1} for n2 >= N2 (compile-time recursion so
-// that every twiddle is a constant expression)
 template <int R, int R1, int S, int N2, int K1>
 __device__ __forceinline__ void twiddle_row(float2* y) {
   if constexpr (K1 < R1) {
@@ -116,7 +120,6 @@ __device__ __forceinline__ void twiddle_row(float2* y) {
     twiddle_row<R, R1, S, N2, K1 + 1>(y);
   }
 }
-
 template <int R, int R1, int R2, int S, int N2>
 __device__ __forceinline__ void twiddle_block(float2* y) {
   if constexpr (N2 < R2) {
@@ -124,6 +127,7 @@ __device__ __forceinline__ void twiddle_block(float2* y) {
     twiddle_block<R, R1, R2, S, N2 + 1>(y);
   }
 }
+
 template <int R, int S>
 __device__ __forceinline__ void dft(float2* v) {
   if constexpr (R == 1) {
@@ -139,7 +143,7 @@ __device__ __forceinline__ void dft(float2* v) {
     float2 t = cadd(b, c);
     float2 d = csub(b, c);
     float2 m = make_float2(fmaf(-0.5f, t.x, a.x), fmaf(-0.5f, t.y, a.y));
-    float2 r = make_float2(-S * h * d.y, S * h * d.x);  // S i h d
+    float2 r = make_float2(-S * h * d.y, S * h * d.x);
     v[0] = cadd(a, t);
     v[1] = cadd(m, r);
     v[2] = csub(m, r);
@@ -166,7 +170,6 @@ __device__ __forceinline__ void dft(float2* v) {
 #pragma unroll
       for (int k1 = 0; k1 < R1; ++k1) y[n2 * R1 + k1] = t[k1];
     }
-    // twiddles w_R^{n2*k1}
     twiddle_block<R, R1, R2, S, 1>(y);
 #pragma unroll
     for (int k1 = 0; k1 < R1; ++k1) {
@@ -181,34 +184,100 @@ __device__ __forceinline__ void dft(float2* v) {
 }
 
 // ---------------------------------------------------------------------------
-// tile addressing
+// shared-memory layouts of the exchanges
 // ---------------------------------------------------------------------------
-template <int W>
-__device__ __forceinline__ int tidx(int l, int c) {
-  return l * W + (c ^ (l & (W - 1)));
+template <int L, int W>
+struct LaySwz {  // column passes
+  static constexpr int SIZE = L * W;
+  static __device__ __forceinline__ int idx(int l, int c) { return l * W + (c ^ (l & (W - 1))); }
+};
+template <int L, int W>
+struct LayPad {  // row passes
+  static constexpr int STRIDE = L + L / 16;
+  static constexpr int SIZE = W * STRIDE;
+  static __device__ __forceinline__ int idx(int l, int c) { return c * STRIDE + l + (l >> 4); }
+};
+
+// ---------------------------------------------------------------------------
+// radix plans.  TPT threads per sequence, E = L/TPT elements per thread;
+// every radix divides E; the first and the last radix are equal.
+// ---------------------------------------------------------------------------
+template <int... Rs>
+struct Radices {
+  static constexpr int count = sizeof...(Rs);
+  static constexpr int value[count] = {Rs...};
+};
+
+template <int L>
+struct Plan;
+// clang-format off
+template <> struct Plan<16>   { static constexpr int TPT = 2;   using R = Radices<4, 4>; };
+template <> struct Plan<32>   { static constexpr int TPT = 4;   using R = Radices<4, 2, 4>; };
+template <> struct Plan<64>   { static constexpr int TPT = 8;   using R = Radices<8, 8>; };
+template <> struct Plan<128>  { static constexpr int TPT = 16;  using R = Radices<4, 8, 4>; };
+template <> struct Plan<256>  { static constexpr int TPT = 32;  using R = Radices<8, 4, 8>; };
+template <> struct Plan<384>  { static constexpr int TPT = 16;  using R = Radices<8, 6, 8>; };
+template <> struct Plan<512>  { static constexpr int TPT = 64;  using R = Radices<8, 8, 8>; };
+template <> struct Plan<768>  { static constexpr int TPT = 32;  using R = Radices<8, 12, 8>; };
+template <> struct Plan<1024> { static constexpr int TPT = 64;  using R = Radices<8, 16, 8>; };
+template <> struct Plan<2048> { static constexpr int TPT = 128; using R = Radices<16, 8, 16>; };
+// clang-format on
+
+// Per-pass twiddle table of a plan: for every pass after the first (NS > 1)
+// entries w[(r-1)*NS + k] = exp(+2 pi i k r / (NS R)), r in [1,R), k in
+// [0,NS), k fastest so that a warp of the row mapping reads consecutive
+// entries.
+template <int L>
+struct TwiddleTable {
+  using Rad = typename Plan<L>::R;
+  __host__ __device__ static constexpr int offset(int pass) {
+    int ns = 1, total = 0;
+    for (int p = 0; p < pass; ++p) {
+      if (p > 0) total += (Rad::value[p] - 1) * ns;
+      ns *= Rad::value[p];
+    }
+    return total;
+  }
+  __host__ __device__ static constexpr int size() {
+    const int s = offset(Rad::count);
+    return s > 0 ? s : 1;
+  }
+};
+
+// Host side: fill the twiddle table of the plan of length L (double
+// precision angles, rounded once to float).
+template <int L>
+void fill_twiddles(float2* out) {
+  using Rad = typename Plan<L>::R;
+  int ns = 1, off = 0;
+  for (int p = 0; p < Rad::count; ++p) {
+    const int R = Rad::value[p];
+    if (p > 0) {
+      for (int r = 1; r < R; ++r)
+        for (int k = 0; k < ns; ++k) {
+          const double a = 2.0 * kPi * (double)k * (double)r / (double)(ns * R);
+          out[off + (r - 1) * ns + k] = make_float2((float)cos(a), (float)sin(a));
+        }
+      off += (R - 1) * ns;
+    }
+    ns *= R;
+  }
 }
 
 // ---------------------------------------------------------------------------
-// One Stockham pass over the tile.  Threads: W * TPT, thread t handles
-// transform c = t % W and butterflies b = t / W + TPT*u.
-// tw[m] = exp(+2 pi i m / L) for m in [0, L).
+// the register-resident transform
+// v[u*R + r] = element at position (j + TPT*u) + r*L/R of the first pass on
+// entry, of the last pass on exit (same positions: first radix == last).
 // ---------------------------------------------------------------------------
-template <int L, int W, int TPT, int S, int NS, int R>
-__device__ __forceinline__ void fft_pass(float2* __restrict__ tile, const float2* __restrict__ tw) {
+template <int L, int TPT, int S, class Lay, int P, int NS>
+__device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf, const float2* __restrict__ tw,
+                                             int c, int j) {
+  using Rad = typename Plan<L>::R;
+  constexpr int R = Rad::value[P];
   constexpr int NB = L / R;
-  static_assert(NB % TPT == 0, "butterflies must divide evenly over the threads");
   constexpr int U = NB / TPT;
-  constexpr int TWS = L / (NS * R);
-  const int c = threadIdx.x % W;
-  const int j = threadIdx.x / W;
-  float2 v[U][R];
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    const int b = j + TPT * u;
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[u][r] = tile[tidx<W>(b + r * NB, c)];
-  }
-  __syncthreads();
+  static_assert(NB % TPT == 0, "butterflies must divide evenly over the threads");
+  constexpr int OFF = TwiddleTable<L>::offset(P);
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     const int b = j + TPT * u;
@@ -216,49 +285,65 @@ __device__ __forceinline__ void fft_pass(float2* __restrict__ tile, const float2
     if constexpr (NS > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        float2 w = tw[k * r * TWS];
+        float2 w = tw[OFF + (r - 1) * NS + k];
         if (S < 0) w.y = -w.y;
-        v[u][r] = cmul(v[u][r], w);
+        v[u * R + r] = cmul(v[u * R + r], w);
       }
     }
-    dft<R, S>(v[u]);
-    const int base = (b / NS) * NS * R + k;
-#pragma unroll
-    for (int q = 0; q < R; ++q) tile[tidx<W>(base + q * NS, c)] = v[u][q];
+    dft<R, S>(v + u * R);
   }
-  __syncthreads();
+  if constexpr (P + 1 < Rad::count) {
+    // exchange: outputs to their Stockham positions, inputs of the next pass
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int b = j + TPT * u;
+      const int k = (NS == 1) ? 0 : (b % NS);
+      const int base = (b / NS) * NS * R + k;
+#pragma unroll
+      for (int q = 0; q < R; ++q) buf[Lay::idx(base + q * NS, c)] = v[u * R + q];
+    }
+    __syncthreads();
+    constexpr int R2 = Rad::value[P + 1];
+    constexpr int NB2 = L / R2;
+    constexpr int U2 = NB2 / TPT;
+    static_assert(U2 * R2 == U * R, "every pass must keep E elements per thread");
+#pragma unroll
+    for (int u = 0; u < U2; ++u) {
+      const int b = j + TPT * u;
+#pragma unroll
+      for (int r = 0; r < R2; ++r) v[u * R2 + r] = buf[Lay::idx(b + r * NB2, c)];
+    }
+    __syncthreads();
+    fft_pass_reg<L, TPT, S, Lay, P + 1, NS * R>(v, buf, tw, c, j);
+  }
 }
 
-template <int L, int W, int TPT, int S, int NS, int R, int... Rest>
-__device__ __forceinline__ void fft_passes(float2* tile, const float2* tw) {
-  fft_pass<L, W, TPT, S, NS, R>(tile, tw);
-  if constexpr (sizeof...(Rest) > 0) fft_passes<L, W, TPT, S, NS * R, Rest...>(tile, tw);
+template <int L, class Lay, int S>
+__device__ __forceinline__ void fft_reg(float2* v, float2* buf, const float2* tw, int c, int j) {
+  using Rad = typename Plan<L>::R;
+  static_assert(Rad::value[0] == Rad::value[Rad::count - 1], "first and last radix must match");
+  fft_pass_reg<L, Plan<L>::TPT, S, Lay, 0, 1>(v, buf, tw, c, j);
 }
 
-// Radix plans: the product of the radices is L; every radix divides the
-// number of elements a thread holds (L / TPT) so that the passes divide
-// evenly over the threads.
 template <int L>
-struct Plan;
-// clang-format off
-template <> struct Plan<8>    { static constexpr int TPT = 1;   template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<8,    W, TPT, S, 1, 8>(t, w); } };
-template <> struct Plan<16>   { static constexpr int TPT = 2;   template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<16,   W, TPT, S, 1, 8, 2>(t, w); } };
-template <> struct Plan<32>   { static constexpr int TPT = 4;   template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<32,   W, TPT, S, 1, 8, 4>(t, w); } };
-template <> struct Plan<64>   { static constexpr int TPT = 8;   template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<64,   W, TPT, S, 1, 8, 8>(t, w); } };
-template <> struct Plan<128>  { static constexpr int TPT = 16;  template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<128,  W, TPT, S, 1, 8, 4, 4>(t, w); } };
-template <> struct Plan<256>  { static constexpr int TPT = 32;  template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<256,  W, TPT, S, 1, 8, 8, 4>(t, w); } };
-template <> struct Plan<384>  { static constexpr int TPT = 16;  template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<384,  W, TPT, S, 1, 8, 8, 6>(t, w); } };
-template <> struct Plan<512>  { static constexpr int TPT = 64;  template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<512,  W, TPT, S, 1, 8, 8, 8>(t, w); } };
-template <> struct Plan<768>  { static constexpr int TPT = 32;  template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<768,  W, TPT, S, 1, 8, 8, 12>(t, w); } };
-template <> struct Plan<1024> { static constexpr int TPT = 64;  template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<1024, W, TPT, S, 1, 16, 8, 8>(t, w); } };
-template <> struct Plan<2048> { static constexpr int TPT = 128; template <int W, int S> __device__ static void run(float2* t, const float2* w) { fft_passes<2048, W, TPT, S, 1, 8, 16, 16>(t, w); } };
-// clang-format on
+struct Elems {
+  static constexpr int value = L / Plan<L>::TPT;
+};
 
-// Tile width (transforms per tile): 16 keeps every access conflict free;
-// 2048-point tiles use 8 to fit in shared memory.
+// Position of element e of thread j (first-pass inputs / last-pass outputs).
+template <int L>
+__device__ __forceinline__ int elem_pos(int e, int j) {
+  constexpr int R = Plan<L>::R::value[0];
+  constexpr int NB = L / R;
+  const int u = e / R, r = e - u * R;
+  return (j + Plan<L>::TPT * u) + r * NB;
+}
+
+// Tile widths (sequences per CTA) of the two passes.
 template <int L>
 struct TileW {
-  static constexpr int value = (L >= 2048) ? 8 : (L < 16 ? L : 16);
+  static constexpr int rows = (L >= 1024) ? 4 : (L >= 256 ? 8 : 16);
+  static constexpr int cols = (L >= 1024) ? 8 : 16;
 };
 
 }  // namespace spe

@@ -5,8 +5,11 @@
 // on x86-64 and aarch64 (GCC contracts a+b*c into fma on aarch64 otherwise).
 #include <cmath>
 #include <cstring>
+#include <random>
 #include <vector>
 
+#include "../../include/spe_engine.h"
+#include "spe_engine_impl.h"
 #include "spe_internal.h"
 
 namespace spe {
@@ -93,4 +96,64 @@ int prepare_pattern(const float* in, int n, int cx, int cy, bool use_bounds, flo
   return 0;
 }
 
+// Solver::Crossover's per-child draws (src/solver.cpp:750-801), in the same
+// order and float arithmetic.  Context::rand(min, max) is
+// distribution(generator)*(max-min)+min with a float uniform distribution
+// (src/context.h:17); its arguments are floats.
+int draw_children(std::mt19937& g, int P, const int* order, float suppdim, int n, float crossbalance, float crossexp,
+                  float crossftin, std::vector<ChildDraw>& out, std::vector<int>& cmaps) {
+  std::uniform_real_distribution<float> dist(0, 1);
+  auto rnd = [&](float lo, float hi) { return dist(g) * (hi - lo) + lo; };
+  out.assign(P, ChildDraw{});
+  cmaps.clear();
+  for (int i = 0; i < P; ++i) {
+    ChildDraw& c = out[i];
+    const int extracted = int(std::pow(rnd(0, 1), crossexp) * float(P));
+    c.p1 = order[extracted];
+    c.p2 = int(rnd(0, P - 0.0001));
+    c.p3 = int(rnd(0, P - 0.0001));
+    c.cft = rnd(0, 1) < crossftin ? 1 : 0;
+    if (c.cft) {
+      c.ssx = int(rnd(std::ceil(float(n) / suppdim), std::ceil(float(n) / 4.)));
+      c.ssy = int(rnd(std::ceil(float(n) / suppdim), std::ceil(float(n) / 4.)));
+    } else {
+      c.ssx = int(rnd(suppdim / 10. + 1., suppdim / 2.));
+      c.ssy = int(rnd(suppdim / 10. + 1., suppdim / 2.));
+    }
+    if (c.ssx < 1 || c.ssy < 1) return 1;
+    c.csx = (n + c.ssx - 1) / c.ssx + 1;
+    c.csy = (n + c.ssy - 1) / c.ssy + 1;
+    c.ox = int(rnd(0, c.ssx));
+    c.oy = int(rnd(0, c.ssy));
+    c.rot = rnd(0, M_PI);
+    c.cmap = (int)cmaps.size();
+    for (int k = 0; k < c.csx * c.csy; ++k) cmaps.push_back(rnd(0, 1) < crossbalance ? 1 : 0);
+  }
+  return 0;
+}
+
 }  // namespace spe
+
+extern "C" int spe_crossover_draws(uint32_t seed, int count, const int32_t* order, float suppdim, int n,
+                                   float crossbalance, float crossexp, float crossft, int32_t* draws, float* rot,
+                                   int32_t* cmaps, int cmaps_capacity, int32_t* cmaps_used) {
+  if (count <= 0 || !order || !draws || !rot || !cmaps_used)
+    return spe_detail::fail(SPE_ERR_INVALID, "invalid crossover draw arguments");
+  std::mt19937 g(seed);
+  std::vector<spe::ChildDraw> d;
+  std::vector<int> cm;
+  if (spe::draw_children(g, count, order, suppdim, n, crossbalance, crossexp, crossft, d, cm))
+    return spe_detail::fail(SPE_ERR_INVALID, "crossover cell size below one pixel");
+  for (int i = 0; i < count; ++i) {
+    const spe::ChildDraw& c = d[i];
+    const int32_t v[11] = {c.p1, c.p2, c.p3, c.cft, c.ssx, c.ssy, c.csx, c.csy, c.ox, c.oy, c.cmap};
+    std::memcpy(draws + 11 * i, v, sizeof v);
+    rot[i] = c.rot;
+  }
+  *cmaps_used = (int32_t)cm.size();
+  if (cmaps) {
+    if ((int)cm.size() > cmaps_capacity) return spe_detail::fail(SPE_ERR_INVALID, "crossmap buffer too small");
+    std::memcpy(cmaps, cm.data(), cm.size() * sizeof(int32_t));
+  }
+  return SPE_OK;
+}

@@ -4,10 +4,28 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <random>
+#include <vector>
+
 namespace spe {
 
 // Host pattern encoding (spe_host.cpp).
 int prepare_pattern(const float* in, int n, int cx, int cy, bool use_bounds, float* out);
+
+// Random draws of one crossover child (Solver::Crossover, src/solver.cpp:750-801).
+struct ChildDraw {
+  int p1, p2, p3;    // parent indices (p1 through the error order)
+  int cft;           // Fourier-space crossover
+  int ssx, ssy;      // cell sizes
+  int csx, csy;      // crossmap cells
+  int ox, oy;        // offsets
+  float rot;         // rotation angle
+  int cmap;          // offset of the child's crossmap in the crossmap pool
+};
+// Draws all children in the reference's order from generator g.  Returns
+// non-zero if a cell size would fall below one pixel.
+int draw_children(std::mt19937& g, int count, const int* order, float suppdim, int n, float crossbalance,
+                  float crossexp, float crossftin, std::vector<ChildDraw>& out, std::vector<int>& cmaps);
 
 // Everything a size-specialised sequence needs about one call.
 struct Ctx {
@@ -33,7 +51,10 @@ struct Gate {
 // Size-specialised operation table (one per compiled pattern size).
 struct SizeOps {
   int n;
-  int tiles_per_individual;  // CTAs per individual of one pass
+  int tiles_rows;  // CTAs per individual of a row pass
+  int tiles_cols;  // CTAs per individual of a column pass
+  int tw_size;     // twiddle table entries
+  void (*fill_tw)(float2*);
   // upd: 0 HIO, 1 RAAR, 2 ER
   cudaError_t (*iterate)(const Ctx&, int upd, int iterations, float beta, Gate g);
   // blurred modulus into M, per-CTA max into partials
@@ -47,6 +68,17 @@ struct SizeOps {
   // sign -1: conj(D) Dref, +1: D Dref; peaks into partials (value, index)
   cudaError_t (*corr_peak)(const Ctx&, const float2* D, const float2* Dref, size_t ref_stride, int ref_first,
                            int sign, float minr, float maxr, int norm_d, int norm_ref, double* partials);
+  // generic transforms over Ctx::count items starting at the given arrays
+  // in-place 2D transform; sign +1: FFT+ unnormalised, -1: FFT- then /N^2
+  cudaError_t (*fft2)(const Ctx&, float2* data, int sign);
+  // M = |FFT+(src)| (tmp: scratch items)
+  cudaError_t (*ft_magnitude)(const Ctx&, const float2* src, float2* tmp, float* M);
+  // dst = FFT+(|src|)
+  cudaError_t (*abs_spectrum_items)(const Ctx&, const float2* src, float2* dst);
+  // peaks (value, index) of |FFT-(cross power of D[xi[p]], Dref[ri[p]])|^2
+  cudaError_t (*corr_peak_idx)(const Ctx&, const float2* D, const float2* Dref, const int* xi, const int* ri,
+                               int sign, float minr, float maxr, int norm_d, int norm_ref, float2* scratch,
+                               double* partials);
 };
 
 const SizeOps* size_ops(int n);

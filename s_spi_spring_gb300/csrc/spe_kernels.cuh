@@ -2,8 +2,8 @@
 //
 // Layout in HBM: the population is P individuals of N x N complex64
 // (interleaved re/im, x fastest, i = x + y*N), individual p at offset p*N*N.
-// A 2D transform is a row pass (transforms along x, 16 rows per CTA) and a
-// column pass (transforms along y, 16 columns per CTA).  One iteration of
+// A 2D transform is a row pass (transforms along x, a few rows per CTA) and
+// a column pass (transforms along y, 16 columns per CTA).  One iteration of
 // HIO / RAAR / ER is
 //   column pass: T -> FFT+ (y) -> masked modulus projection -> FFT- (y) -> T
 //   row pass:    T -> FFT- (x) -> /N^2 -> support update with rho, S -> rho
@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 #include "spe_fft.cuh"
 
@@ -138,88 +140,75 @@ __device__ __forceinline__ void block_argmax_store(double* __restrict__ partials
 
 // ---------------------------------------------------------------------------
 // the pass kernel
+//
+// Row pass (AXIS == AX_ROWS): a CTA owns W consecutive rows of one
+// individual; thread t handles row c = t / TPT, positions x = elem_pos(e, j)
+// with j = t % TPT, so each warp reads and writes 256-byte row segments.
+// Column pass: a CTA owns W consecutive columns; thread t handles column
+// c = t % W, positions y = elem_pos(e, j) with j = t / W, so a warp covers
+// W-element row segments of consecutive rows.
 // ---------------------------------------------------------------------------
-struct TileGeom {
-  int p;   // individual (absolute slot)
-  int y0;  // first row of the tile (row pass) or 0
-  int x0;  // first column of the tile (column pass) or 0
+template <int N, int AXIS>
+struct PassCfg {
+  static constexpr int W = (AXIS == AX_ROWS) ? TileW<N>::rows : TileW<N>::cols;
+  static constexpr int TPT = Plan<N>::TPT;
+  static constexpr int NT = W * TPT;
+  static constexpr int E = Elems<N>::value;
+  static constexpr int TWN = (TwiddleTable<N>::size() + 1) & ~1;
+  using Lay = typename std::conditional<AXIS == AX_ROWS, LayPad<N, W>, LaySwz<N, W>>::type;
+  static constexpr size_t SMEM = (size_t)(TWN + Lay::SIZE) * sizeof(float2);
 };
 
-template <int N, int AXIS>
-__device__ __forceinline__ TileGeom tile_geom(int first) {
-  constexpr int W = TileW<N>::value;
-  constexpr int TPI = N / W;  // tiles per individual
-  TileGeom g;
-  g.p = first + blockIdx.x / TPI;
-  const int t = blockIdx.x % TPI;
-  g.y0 = (AXIS == AX_ROWS) ? t * W : 0;
-  g.x0 = (AXIS == AX_COLS) ? t * W : 0;
-  return g;
-}
-
-// Element i of the staging loops -> (l, c) of the tile and (y, x) of the
-// individual.  Row pass: consecutive i walk along x of one row (coalesced
-// global access, conflict-free swizzled stores).  Column pass: consecutive i
-// walk along the W columns of one row, then down the rows.
-template <int N, int AXIS>
-__device__ __forceinline__ void stage_coords(int i, const TileGeom& g, int& l, int& c, int& y, int& x) {
-  constexpr int W = TileW<N>::value;
-  if (AXIS == AX_ROWS) {
-    c = i / N;
-    l = i - c * N;
-    y = g.y0 + c;
-    x = l;
-  } else {
-    l = i / W;
-    c = i - l * W;
-    y = l;
-    x = g.x0 + c;
-  }
-}
-
 template <int N, int AXIS, class Op>
-__global__ void __launch_bounds__(TileW<N>::value * Plan<N>::TPT)
+__global__ void __launch_bounds__(PassCfg<N, AXIS>::NT)
     pass_kernel(const Op op, const float2* __restrict__ twg) {
-  constexpr int W = TileW<N>::value;
-  constexpr int NT = W * Plan<N>::TPT;
+  using C = PassCfg<N, AXIS>;
+  constexpr int W = C::W, TPT = C::TPT, NT = C::NT, E = C::E;
   extern __shared__ float2 smem[];
-  float2* tile = smem;
-  float2* tw = smem + N * W;
-  for (int i = threadIdx.x; i < N; i += NT) tw[i] = twg[i];
+  float2* tw = smem;
+  float2* buf = smem + C::TWN;
+  constexpr int TWS = TwiddleTable<N>::size();
+  for (int i = threadIdx.x; i < TWS; i += NT) tw[i] = twg[i];
 
-  const TileGeom g = tile_geom<N, AXIS>(op.first);
-  const size_t base = (size_t)g.p * N * N;
+  const int t = threadIdx.x;
+  const int c = (AXIS == AX_ROWS) ? t / TPT : t % W;
+  const int j = (AXIS == AX_ROWS) ? t % TPT : t / W;
+  constexpr int TPI = N / W;  // tiles per individual
+  const int p = op.first + blockIdx.x / TPI;
+  const int fixed = (blockIdx.x % TPI) * W + c;  // row (row pass) or column (column pass)
+  const size_t base = (size_t)p * N * N;
   typename Op::Acc acc;
 
-#pragma unroll 4
-  for (int i = threadIdx.x; i < N * W; i += NT) {
-    int l, c, y, x;
-    stage_coords<N, AXIS>(i, g, l, c, y, x);
-    tile[tidx<W>(l, c)] = op.load(base + (size_t)y * N + x, g.p, y, x, acc);
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int l = elem_pos<N>(e, j);
+    const int y = (AXIS == AX_ROWS) ? fixed : l;
+    const int x = (AXIS == AX_ROWS) ? l : fixed;
+    v[e] = op.load(base + (size_t)y * N + x, p, y, x, acc);
   }
-  __syncthreads();
-  if constexpr (Op::FFT1 != 0) Plan<N>::template run<W, Op::FFT1>(tile, tw);
+  if constexpr (Op::FFT1 != 0) fft_reg<N, typename C::Lay, Op::FFT1>(v, buf, tw, c, j);
   if constexpr (Op::FFT2 != 0) {
-#pragma unroll 4
-    for (int i = threadIdx.x; i < N * W; i += NT) {
-      int l, c, y, x;
-      stage_coords<N, AXIS>(i, g, l, c, y, x);
-      const int t = tidx<W>(l, c);
-      tile[t] = op.mid(tile[t], base + (size_t)y * N + x, g.p, y, x, acc);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int l = elem_pos<N>(e, j);
+      const int y = (AXIS == AX_ROWS) ? fixed : l;
+      const int x = (AXIS == AX_ROWS) ? l : fixed;
+      v[e] = op.mid(v[e], base + (size_t)y * N + x, p, y, x, acc);
     }
-    __syncthreads();
-    Plan<N>::template run<W, Op::FFT2>(tile, tw);
+    fft_reg<N, typename C::Lay, Op::FFT2>(v, buf, tw, c, j);
   }
-#pragma unroll 4
-  for (int i = threadIdx.x; i < N * W; i += NT) {
-    int l, c, y, x;
-    stage_coords<N, AXIS>(i, g, l, c, y, x);
-    op.store(tile[tidx<W>(l, c)], base + (size_t)y * N + x, g.p, y, x, acc);
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int l = elem_pos<N>(e, j);
+    const int y = (AXIS == AX_ROWS) ? fixed : l;
+    const int x = (AXIS == AX_ROWS) ? l : fixed;
+    op.store(v[e], base + (size_t)y * N + x, p, y, x, acc);
   }
   if constexpr (Op::NSUM + Op::NMAX > 0) {
-    double v[NRED];
-    acc.values(v);
-    block_reduce_store<NT, Op::NSUM, Op::NMAX>(op.partials, v);
+    double r[NRED];
+    acc.values(r);
+    block_reduce_store<NT, Op::NSUM, Op::NMAX>(op.partials, r);
   }
   if constexpr (Op::PEAK) block_argmax_store<NT>(op.partials, acc.mx, acc.idx);
 }
@@ -564,6 +553,66 @@ struct OpRowsPeak : OpBase {
       a.idx = i;
     }
   }
+};
+
+// ---- generic 2D transforms on arrays of items (item p at offset p*N*N)
+
+// column pass: src -> FFT(S) (y) -> dst
+template <int S>
+struct OpColsTransform : OpBase {
+  static constexpr int FFT1 = S, FFT2 = 0;
+  const float2* src;
+  float2* dst;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return src[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { dst[gi] = v; }
+};
+
+// column pass: src -> FFT+ (y) -> |.| -> M (float)
+struct OpColsMagnitude : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = 0;
+  const float2* src;
+  float* M;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return src[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { M[gi] = cabsf2(v); }
+};
+
+// column pass over pairs: item p forms the band-passed cross-power spectrum
+// of D[xi[p]] with Dref[ri[p]] (conj(D) Dref for SIGN=-1, D Dref for +1;
+// multiply() of gpu_context.cu:1157-1200), masked where A < 0, then
+// FFT- (y) -> dst[p].  Items are numbered from 0 (first == 0).
+template <int SIGN>
+struct OpColsCrossPowerIdx : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0;
+  const float2* D;
+  const float2* Dref;
+  const int* xi;
+  const int* ri;
+  float2* dst;
+  const float* A;
+  int n;
+  float minr, maxr;
+  int norm_d, norm_ref;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int p, int y, int x, Acc&) const {
+    const size_t npix = (size_t)n * n;
+    const size_t pix = (size_t)y * n + x;
+    float2 d = D[(size_t)__ldg(xi + p) * npix + pix];
+    float2 r = Dref[(size_t)__ldg(ri + p) * npix + pix];
+    if (norm_d) d = ft_shift_norm(d);
+    if (norm_ref) r = ft_shift_norm(r);
+    const float sd = (float)SIGN * d.y;
+    float2 c = make_float2(d.x * r.x - sd * r.y, d.x * r.y + sd * r.x);
+    const float w = bandpass2(x, y, n, minr, maxr);
+    c = make_float2(c.x * w, c.y * w);
+    if (__ldg(A + pix) < 0.f) c = make_float2(0.f, 0.f);
+    return c;
+  }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { dst[gi] = v; }
 };
 
 }  // namespace spe

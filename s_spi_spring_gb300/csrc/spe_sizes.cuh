@@ -8,11 +8,12 @@ namespace spe {
 
 template <int N, int AXIS, class Op>
 cudaError_t launch_pass(const Op& op, int count, cudaStream_t st, const float2* tw) {
-  constexpr int W = TileW<N>::value;
-  constexpr int NT = W * Plan<N>::TPT;
+  using C = PassCfg<N, AXIS>;
+  constexpr int W = C::W;
+  constexpr int NT = C::NT;
   // the block reductions shuffle with a full warp mask
   static_assert(NT % 32 == 0, "pass kernels need whole warps");
-  const size_t smem = (size_t)(N * W + N) * sizeof(float2);
+  const size_t smem = C::SMEM;
   auto kern = pass_kernel<N, AXIS, Op>;
   // the dynamic shared-memory opt-in is per device and per kernel
   static unsigned long long configured = 0ull;
@@ -186,14 +187,111 @@ struct SizeImpl {
     return corr_peak_t<+1>(c, D, Dref, ref_stride, ref_first, minr, maxr, norm_d, norm_ref, partials);
   }
 
+
+  // ---- generic transforms over `c.count` items starting at `data` (c.first ignored)
+  static cudaError_t fft2(const Ctx& c, float2* data, int sign) {
+    if (sign > 0) {
+      Ctx z = c;
+      z.first = 0;
+      SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(z, data, data, Gate{0.f, 0.f}, nullptr), c.count, c.st, c.tw)));
+      OpColsTransform<+1> ct;
+      ct.first = 0;
+      ct.partials = nullptr;
+      ct.src = data;
+      ct.dst = data;
+      return launch_pass<N, AX_COLS>(ct, c.count, c.st, c.tw);
+    }
+    OpColsTransform<-1> ct;
+    ct.first = 0;
+    ct.partials = nullptr;
+    ct.src = data;
+    ct.dst = data;
+    SPE_TRY((launch_pass<N, AX_COLS>(ct, c.count, c.st, c.tw)));
+    OpRowsFinal fin;
+    fin.first = 0;
+    fin.partials = nullptr;
+    fin.T = data;
+    fin.out = data;
+    fin.scale = scale();
+    return launch_pass<N, AX_ROWS>(fin, c.count, c.st, c.tw);
+  }
+
+  // M[p] = |FFT+(src[p])| (2D), tmp: scratch of count items
+  static cudaError_t ft_magnitude(const Ctx& c, const float2* src, float2* tmp, float* M) {
+    Ctx z = c;
+    z.first = 0;
+    SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(z, src, tmp, Gate{0.f, 0.f}, nullptr), c.count, c.st, c.tw)));
+    OpColsMagnitude cm;
+    cm.first = 0;
+    cm.partials = nullptr;
+    cm.src = tmp;
+    cm.M = M;
+    return launch_pass<N, AX_COLS>(cm, c.count, c.st, c.tw);
+  }
+
+  // dst[p] = FFT+(|src[p]|) (2D)
+  static cudaError_t abs_spectrum_items(const Ctx& c, const float2* src, float2* dst) {
+    Ctx z = c;
+    z.first = 0;
+    SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_ABS>(z, src, dst, Gate{0.f, 0.f}, nullptr), c.count, c.st, c.tw)));
+    OpColsTransform<+1> ct;
+    ct.first = 0;
+    ct.partials = nullptr;
+    ct.src = dst;
+    ct.dst = dst;
+    return launch_pass<N, AX_COLS>(ct, c.count, c.st, c.tw);
+  }
+
+  template <int SIGN>
+  static cudaError_t corr_peak_idx_t(const Ctx& c, const float2* D, const float2* Dref, const int* xi, const int* ri,
+                                     float minr, float maxr, int norm_d, int norm_ref, float2* scratch,
+                                     double* partials) {
+    OpColsCrossPowerIdx<SIGN> cp;
+    cp.first = 0;
+    cp.partials = nullptr;
+    cp.D = D;
+    cp.Dref = Dref;
+    cp.xi = xi;
+    cp.ri = ri;
+    cp.dst = scratch;
+    cp.A = c.A;
+    cp.n = N;
+    cp.minr = minr;
+    cp.maxr = maxr;
+    cp.norm_d = norm_d;
+    cp.norm_ref = norm_ref;
+    SPE_TRY((launch_pass<N, AX_COLS>(cp, c.count, c.st, c.tw)));
+    OpRowsPeak pk;
+    pk.first = 0;
+    pk.partials = partials;
+    pk.T = scratch;
+    pk.n = N;
+    return launch_pass<N, AX_ROWS>(pk, c.count, c.st, c.tw);
+  }
+
+  // peaks of item p: correlation of D[xi[p]] with Dref[ri[p]], c.count items
+  static cudaError_t corr_peak_idx(const Ctx& c, const float2* D, const float2* Dref, const int* xi, const int* ri,
+                                   int sign, float minr, float maxr, int norm_d, int norm_ref, float2* scratch,
+                                   double* partials) {
+    if (sign < 0) return corr_peak_idx_t<-1>(c, D, Dref, xi, ri, minr, maxr, norm_d, norm_ref, scratch, partials);
+    return corr_peak_idx_t<+1>(c, D, Dref, xi, ri, minr, maxr, norm_d, norm_ref, scratch, partials);
+  }
+
   static const SizeOps* table() {
     static const SizeOps t = {N,
-                              N / TileW<N>::value,
+                              N / TileW<N>::rows,
+                              N / TileW<N>::cols,
+                              TwiddleTable<N>::size(),
+                              &fill_twiddles<N>,
                               &SizeImpl<N>::iterate,
                               &SizeImpl<N>::blur_magnitude,
                               &SizeImpl<N>::error_terms,
                               &SizeImpl<N>::abs_spectrum,
-                              &SizeImpl<N>::corr_peak};
+                              &SizeImpl<N>::corr_peak,
+                              &SizeImpl<N>::fft2,
+                              &SizeImpl<N>::ft_magnitude,
+                              &SizeImpl<N>::abs_spectrum_items,
+                              &SizeImpl<N>::corr_peak_idx};
     return &t;
   }
 };

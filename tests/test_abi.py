@@ -68,3 +68,29 @@ def test_prepare_pattern_encodings():
     known = I >= 0
     assert np.allclose(np.fft.ifftshift(np.where(known, np.sqrt(np.maximum(I, 0)), 0))[np.fft.ifftshift(known)],
                        A[np.fft.ifftshift(known)])
+
+
+@pytest.mark.parametrize("seed,P,crossft,crossexp", [(17, 16, 1.0, 1.0), (42, 33, 0.5, 2.0), (7, 8, 0.0, 0.7)])
+def test_crossover_draws_match_oracle(seed, P, crossft, crossexp):
+    """The engine's host-side crossover draws follow Solver::Crossover's order
+    (src/solver.cpp:750-801) with the libstdc++ generator pinned in
+    tests/golden/rng_std.json."""
+    rng = np.random.default_rng(seed)
+    errors = rng.uniform(0.1, 0.5, P).astype(np.float32)
+    order = o.sorted_indexes(errors)
+    n = 128
+    best = np.zeros((n, n), np.int32)
+    best[40:80, 50:70] = 1
+    suppdim = o.suppdim_of(best, n)
+    draws, rot, cm = _lib.crossover_draws(seed, order, suppdim, n, 0.6, crossexp, crossft)
+    ref = o.draw_crossover(o.ContextRNG(seed), P, order, suppdim, n, 0.6, crossexp, crossft)
+    off = 0
+    for i, d in enumerate(ref):
+        got = draws[i].tolist()
+        assert got[:10] == [d.p1, d.p2, d.p3, int(d.crossft), d.squaresizex, d.squaresizey, d.crosssizex,
+                            d.crosssizey, d.offsetx, d.offsety], i
+        assert np.float32(rot[i]) == np.float32(d.rotangle)
+        assert got[10] == off
+        assert np.array_equal(cm[off:off + d.crossmap.size], d.crossmap)
+        off += d.crossmap.size
+    assert off == cm.size
