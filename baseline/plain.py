@@ -1,0 +1,67 @@
+"""Build, load and time the plain per-individual cuFFT path
+(``baseline/plain_cufft.cu``): the reference's execution structure with one
+stream, one cuFFT plan and separate kernels per context, individuals spread
+over OpenMP host threads."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_build" / "libspe_plain.so"
+_lib = None
+
+
+def build(verbose=False) -> Path:
+    OUT.parent.mkdir(exist_ok=True)
+    src = HERE / "plain_cufft.cu"
+    if OUT.exists() and OUT.stat().st_mtime > max(src.stat().st_mtime, Path(__file__).stat().st_mtime):
+        return OUT
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
+           "-Xcompiler", "-fPIC,-fopenmp", "-o", str(OUT), str(src), "-lcufft", "-lgomp"]
+    subprocess.check_call(cmd)
+    if verbose:
+        print(f"built {OUT}")
+    return OUT
+
+
+def load():
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(str(build()))
+        lib.plain_create.restype = C.c_void_p
+        lib.plain_create.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int]
+        lib.plain_destroy.argtypes = [C.c_void_p]
+        lib.plain_iterate.restype = C.c_int
+        lib.plain_iterate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
+                                      C.c_float, C.c_int]
+        _lib = lib
+    return _lib
+
+
+class Plain:
+    def __init__(self, A, nctx=8, device=0):
+        self.lib = load()
+        A = np.ascontiguousarray(A, dtype=np.float32)
+        self.n = A.shape[0]
+        self.h = self.lib.plain_create(self.n, A.ctypes.data, int(nctx), int(device))
+        if not self.h:
+            raise RuntimeError("plain baseline: context creation failed")
+
+    def close(self):
+        if self.h:
+            self.lib.plain_destroy(self.h)
+            self.h = None
+
+    def iterate(self, rho_ptr, S_ptr, count, iters, upd, beta, real=0.0, copies=True):
+        rc = self.lib.plain_iterate(self.h, rho_ptr, S_ptr, int(count), int(iters), int(upd), float(beta),
+                                    float(real), int(bool(copies)))
+        if rc:
+            raise RuntimeError("plain baseline: CUDA error")

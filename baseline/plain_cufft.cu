@@ -1,0 +1,200 @@
+// Plain per-individual GPU path: the reference's execution structure,
+// restated for measurement (MEASUREMENT INFRASTRUCTURE, not the engine).
+//
+// Mirrors MasterSPP/S_SPI_SPRING's Solver::RAAR/HIO/ER (src/solver.cpp:360-411)
+// driving GPU_context (src/gpu/gpu_context.h:17-84, gpu_context.cu:778-902):
+// OpenMP host threads, each owning one context = one non-blocking stream, one
+// cuFFT C2C plan (batch 1) and device buffers; per individual: staged H2D
+// copies, then per iteration cuFFT INVERSE, the masked modulus projection, cuFFT
+// FORWARD, /N^2 and the support update as separate 32x32-thread kernels, the
+// trailing projection, a stream synchronisation and staged D2H copies.  With
+// `copies` == 0 the population stays in device memory and only the kernels
+// and transforms run (the device-resident comparison).
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <math.h>
+#include <omp.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+namespace {
+
+__device__ __forceinline__ bool gate_out(float2 v, float thi, float tlo) {
+  const float ph = atan2f(v.y, v.x);
+  return (ph > thi) || (ph < -tlo);
+}
+
+__global__ void k_project(float2* d, const float* A, int n) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= n || iy >= n) return;
+  const int i = ix + iy * n;
+  const float a = A[i];
+  const float2 v = d[i];
+  const float m = sqrtf(v.y * v.y + v.x * v.x);
+  if (a >= 0.f) {
+    if (m > 0.f) {
+      d[i] = make_float2(a * v.x / m, a * v.y / m);
+    } else {
+      const float ph = atan2f(v.y, v.x);
+      d[i] = make_float2(a * cosf(ph), a * sinf(ph));
+    }
+  } else if (a < -1.5f && m > -a - 2.f) {
+    const float b = -a - 2.f;
+    d[i] = make_float2(b * v.x / m, b * v.y / m);
+  }
+}
+
+__global__ void k_scale(float2* d, int n) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= n || iy >= n) return;
+  const int i = ix + iy * n;
+  const float s = (float)(n * n);
+  d[i] = make_float2(d[i].x / s, d[i].y / s);
+}
+
+// upd: 0 HIO, 1 RAAR, 2 ER
+__global__ void k_update(float2* d, const int* S, float2* buf, float beta, int n, int upd, float thi, float tlo) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= n || iy >= n) return;
+  const int i = ix + iy * n;
+  const float2 rp = d[i];
+  float2 r;
+  if (upd == 2) {
+    const float t = gate_out(rp, thi, tlo) ? 0.f : (float)S[i];
+    r = make_float2(rp.x * t, rp.y * t);
+  } else if (upd == 0) {
+    const float t = gate_out(rp, thi, tlo) ? 0.f : (float)S[i];
+    const float2 b = buf[i];
+    r = make_float2((b.x - beta * rp.x) * (1.f - t) + rp.x * t, (b.y - beta * rp.y) * (1.f - t) + rp.y * t);
+    buf[i] = r;
+  } else {
+    const float2 b = buf[i];
+    const float2 refl = make_float2(2.f * rp.x - b.x, 2.f * rp.y - b.y);
+    if (S[i] == 0 || gate_out(refl, thi, tlo))
+      r = make_float2(beta * b.x + (1.f - 2.f * beta) * rp.x, beta * b.y + (1.f - 2.f * beta) * rp.y);
+    else
+      r = rp;
+    buf[i] = r;
+  }
+  d[i] = r;
+}
+
+struct Ctx {
+  cudaStream_t st = nullptr;
+  cufftHandle plan = 0;
+  float2* rho = nullptr;  // working density (copies mode)
+  int* S = nullptr;
+  float2* buf = nullptr;
+  float2* h_rho = nullptr;  // pinned staging
+  int* h_S = nullptr;
+};
+
+struct Plain {
+  int n = 0, dev = 0;
+  float* A = nullptr;
+  std::vector<Ctx> ctx;
+};
+
+float largest_float_not_above(double t) {
+  float f = (float)t;
+  if ((double)f > t) f = nextafterf(f, -INFINITY);
+  return f;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* plain_create(int n, const float* amp, int nctx, int device) {
+  if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+  Plain* p = new Plain();
+  p->n = n;
+  p->dev = device;
+  const size_t np = (size_t)n * n;
+  cudaMalloc(&p->A, np * sizeof(float));
+  cudaMemcpy(p->A, amp, np * sizeof(float), cudaMemcpyHostToDevice);
+  p->ctx.resize(nctx);
+  for (Ctx& c : p->ctx) {
+    cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking);
+    cufftPlan2d(&c.plan, n, n, CUFFT_C2C);
+    cufftSetStream(c.plan, c.st);
+    cudaMalloc(&c.rho, np * sizeof(float2));
+    cudaMalloc(&c.S, np * sizeof(int));
+    cudaMalloc(&c.buf, np * sizeof(float2));
+    cudaMallocHost(&c.h_rho, np * sizeof(float2));
+    cudaMallocHost(&c.h_S, np * sizeof(int));
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) return nullptr;
+  return p;
+}
+
+void plain_destroy(void* h) {
+  Plain* p = (Plain*)h;
+  if (!p) return;
+  cudaSetDevice(p->dev);
+  for (Ctx& c : p->ctx) {
+    cufftDestroy(c.plan);
+    cudaStreamDestroy(c.st);
+    cudaFree(c.rho);
+    cudaFree(c.S);
+    cudaFree(c.buf);
+    cudaFreeHost(c.h_rho);
+    cudaFreeHost(c.h_S);
+  }
+  cudaFree(p->A);
+  delete p;
+}
+
+// Runs `iterations` of HIO/RAAR/ER (upd 0/1/2) on `count` individuals.
+// copies != 0: rho/S are host arrays, staged per individual like the
+// reference.  copies == 0: rho/S are device arrays (count*n*n) processed in
+// place.  Returns 0 on success.
+int plain_iterate(void* h, float* rho, int32_t* S, int count, int iterations, int upd, float beta, float real,
+                  int copies) {
+  Plain* p = (Plain*)h;
+  const int n = p->n;
+  const size_t np = (size_t)n * n;
+  const double t = (double)(1.f - real) * M_PI;
+  const float thi = upd == 1 ? largest_float_not_above((1.0 - (double)real) * M_PI) : largest_float_not_above(t);
+  const float tlo = largest_float_not_above(t);
+  const dim3 block(32, 32), grid((n + 31) / 32, (n + 31) / 32);
+  int err = 0;
+#pragma omp parallel for schedule(dynamic) num_threads((int)p->ctx.size())
+  for (int irec = 0; irec < count; ++irec) {
+    cudaSetDevice(p->dev);
+    Ctx& c = p->ctx[omp_get_thread_num()];
+    float2* d = c.rho;
+    int* s = c.S;
+    if (copies) {
+      memcpy(c.h_rho, rho + 2 * np * irec, np * sizeof(float2));
+      cudaMemcpyAsync(c.rho, c.h_rho, np * sizeof(float2), cudaMemcpyHostToDevice, c.st);
+      memcpy(c.h_S, S + np * irec, np * sizeof(int));
+      cudaMemcpyAsync(c.S, c.h_S, np * sizeof(int), cudaMemcpyHostToDevice, c.st);
+    } else {
+      d = (float2*)rho + np * irec;
+      s = S + np * irec;
+    }
+    cudaMemcpyAsync(c.buf, d, np * sizeof(float2), cudaMemcpyDeviceToDevice, c.st);
+    for (int it = 0; it <= iterations; ++it) {
+      cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_INVERSE);
+      k_project<<<grid, block, 0, c.st>>>(d, p->A, n);
+      cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_FORWARD);
+      k_scale<<<grid, block, 0, c.st>>>(d, n);
+      if (it < iterations) k_update<<<grid, block, 0, c.st>>>(d, s, c.buf, beta, n, upd, thi, tlo);
+    }
+    if (copies) {
+      cudaMemcpyAsync(c.h_rho, c.rho, np * sizeof(float2), cudaMemcpyDeviceToHost, c.st);
+      cudaMemcpyAsync(c.h_S, c.S, np * sizeof(int), cudaMemcpyDeviceToHost, c.st);
+    }
+    if (cudaStreamSynchronize(c.st) != cudaSuccess) err = 1;
+    if (copies) {
+      memcpy(rho + 2 * np * irec, c.h_rho, np * sizeof(float2));
+      memcpy(S + np * irec, c.h_S, np * sizeof(int));
+    }
+  }
+  return err;
+}
+
+}  // extern "C"

@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=2)
     return ap.parse_args()
 
 
@@ -132,6 +134,46 @@ def cpu_baseline(sample_s: float, threads: int | None = None):
     from oracle import cpu_port
     A, dens, S = workload()
     return cpu_port.time_raar(A, dens, S, BETA, sample_s, threads=threads)
+
+
+def plain_gpu(args, A, dens, S, local, eng):
+    """The plain per-individual cuFFT path (8 contexts, the reference's
+    structure) on the same population, device resident and with the
+    reference's staged host copies; and the R-factor both reach from the
+    same start."""
+    import torch
+    from baseline import plain
+    pl = plain.Plain(A, nctx=8, device=local)
+    dev = f"cuda:{local}"
+    d_rho = torch.from_numpy(dens.view(np.float32).copy()).to(dev)
+    d_S = torch.from_numpy(S.copy()).to(dev)
+    pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, 5, 1, BETA, 0.0, copies=False)
+    torch.cuda.synchronize()
+    d_rho.copy_(torch.from_numpy(dens.view(np.float32).copy()).to(dev))
+    t0 = time.perf_counter()
+    for _ in range(args.plain_steps):
+        pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, args.iters, 1, BETA, 0.0, copies=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    value = args.plain_steps * POP * args.iters / dt
+    # R-factor after one step from the original start, evaluated by the engine
+    h_rho = dens.copy()
+    h_S = S.copy()
+    t0 = time.perf_counter()
+    pl.iterate(h_rho.ctypes.data, h_S.ctypes.data, POP, args.iters, 1, BETA, 0.0, copies=True)
+    dt_e2e = time.perf_counter() - t0
+    pl.close()
+    eng.upload(0, h_rho, S)
+    r_plain = [m["error_fourier"] for m in eng.evaluate(0, POP, 0.0, 0.0)]
+    eng.upload(0, dens, S)
+    eng.raar(0, POP, args.iters, BETA, 0.0)
+    r_eng = [m["error_fourier"] for m in eng.evaluate(0, POP, 0.0, 0.0)]
+    return {"value": round(value, 1), "unit": "iter*individuals/s",
+            "e2e": round(POP * args.iters / dt_e2e, 1), "contexts": 8,
+            "what": "per-individual cuFFT C2C pair + projection, /N^2 and update kernels (32x32 blocks) per "
+                    "iteration on 8 streams / OpenMP threads, as the reference's Solver drives GPU_context",
+            "rfactor_after_step": {"engine_mean": float(np.mean(r_eng)), "plain_mean": float(np.mean(r_plain)),
+                                   "max_abs_diff": float(np.max(np.abs(np.array(r_eng) - np.array(r_plain))))}}
 
 
 def run_engine(args):
@@ -256,6 +298,12 @@ def run_engine(args):
         "gpu_launches": args.steps * (2 * args.iters + 3),
         "clocks": clocks.summary(),
     }
+    if rank == 0 and not args.no_plain:
+        try:
+            out["plain_gpu"] = plain_gpu(args, A, dens, S, local, eng)
+            out["plain_gpu"]["fused_over_plain"] = round(value / world / out["plain_gpu"]["value"], 3)
+        except Exception as ex:
+            out["plain_gpu"] = {"error": str(ex)[:200]}
     if rank == 0 and not args.no_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline(args.cpu_sample_s)

@@ -1,0 +1,120 @@
+// Driver of the reference's own host code (TEST INFRASTRUCTURE).
+//
+// Compiled together with MasterSPP/S_SPI_SPRING src/solver.cpp, taken from
+// where it lies in the reference checkout (see build_ref.py), into
+// oracle/_ref/libref_driver.so.  It runs the reference's Solver on the CPU and
+// exposes what its host code computes:
+//   * the pattern encoding of the Solver constructor (set_boundaries +
+//     prepare, src/solver.cpp:9-52, 173-289), read from Solver::pattern;
+//   * the host side of Solver::Crossover (src/solver.cpp:716-817): order by
+//     error, suppdim, parent choice and every random draw.  A recording
+//     Context (this file's own class, not reference code) is installed in
+//     place of the GPU contexts; it identifies the parents passed to
+//     set_parents_density by a marker value each individual carries and
+//     records the arguments of get_new_individual.
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "solver.h"
+
+namespace {
+
+struct ChildRecord {
+  int self = -1, p1 = -1, p2 = -1, p3 = -1;
+  int crossft = 0, ssx = 0, ssy = 0, csx = 0, csy = 0, ox = 0, oy = 0;
+  float rot = 0.f;
+  std::vector<int> cmap;
+};
+
+// Individual k carries density[0] = (k, 0.5): the marker survives the copies
+// Solver::Crossover makes of its reconstructions.
+int marker(const COMPLEX* d) { return (int)d[0].real(); }
+
+class RecordingContext : public Context {
+ public:
+  RecordingContext(int n, int seed) : Context(n, seed), density((size_t)n * n) {}
+  void set_density(COMPLEX* d) override { std::memcpy(density.data(), d, density.size() * sizeof(COMPLEX)); }
+  void get_density(COMPLEX* d) override { std::memcpy(d, density.data(), density.size() * sizeof(COMPLEX)); }
+  void set_parents_density(COMPLEX* d1, COMPLEX* d2, COMPLEX* d3, COMPLEX*, COMPLEX*) override {
+    cur.self = marker(density.data());
+    cur.p1 = marker(d1);
+    cur.p2 = marker(d2);
+    cur.p3 = marker(d3);
+  }
+  void get_new_individual(SUPPORTTYPE* crossmap, int csx, int csy, int ssx, int ssy, int ox, int oy, FLOAT rot,
+                          FLOAT, FLOAT, bool crossft, bool, FLOAT) override {
+    cur.crossft = crossft;
+    cur.ssx = ssx;
+    cur.ssy = ssy;
+    cur.csx = csx;
+    cur.csy = csy;
+    cur.ox = ox;
+    cur.oy = oy;
+    cur.rot = rot;
+    cur.cmap.assign(crossmap, crossmap + (size_t)csx * csy);
+    records.push_back(cur);
+  }
+  std::vector<COMPLEX> density;
+  ChildRecord cur;
+  std::vector<ChildRecord> records;
+};
+
+}  // namespace
+
+extern "C" {
+
+// Solver(pattern, center, ...) -> Solver::pattern (the encoded amplitudes)
+int ref_prepare_pattern(const float* intensities, int n, int cx, int cy, int use_bounds, float* out) {
+  std::vector<FLOAT> pat(intensities, intensities + (size_t)n * n);
+  Solver s(pat.data(), {(size_t)n, (size_t)n}, {cx, cy}, 0, 0, 0, use_bounds != 0, std::vector<int>{}, 17);
+  std::memcpy(out, s.pattern.data(), (size_t)n * n * sizeof(float));
+  return 0;
+}
+
+// Runs Solver::Crossover on `count` individuals of side n whose errors and
+// supports are given, with one recording context seeded like the reference's
+// first context ((0+1)*seed).  Outputs per child:
+//   draws[11*i .. ] = p1, p2, p3, crossft, ssx, ssy, csx, csy, ox, oy, self
+//   rot[i]; crossmaps concatenated into cmaps (capacity cmaps_cap).
+// Returns the number of crossmap entries, or -1.
+int ref_crossover_draws(int n, int count, const float* errors, const int32_t* best_support, int seed,
+                        float crossbalance, float crossexp, float crossft, int32_t* draws, float* rot, int32_t* cmaps,
+                        int cmaps_cap) {
+  std::vector<FLOAT> pat((size_t)n * n, 1.f);
+  Solver s(pat.data(), {(size_t)n, (size_t)n}, {-1, -1}, 0, 0, 1, false, std::vector<int>{}, seed);
+  for (auto* c : s.contexts) delete c;
+  s.contexts.clear();
+  auto* rc = new RecordingContext(n, 1 * seed);
+  s.contexts.push_back(rc);
+  s.nthreads = 1;
+  const size_t np = (size_t)n * n;
+  std::vector<std::shared_ptr<Reconstruction>> recs;
+  std::vector<COMPLEX> d(np, COMPLEX(0, 0));
+  std::vector<SUPPORTTYPE> sup(np, 0);
+  for (int k = 0; k < count; ++k) {
+    d[0] = COMPLEX((FLOAT)k, 0.5f);
+    auto r = std::make_shared<Reconstruction>(d.data(), sup.data(), std::array<std::size_t, 2>{(size_t)n, (size_t)n});
+    r->error = errors[k];
+    recs.push_back(r);
+  }
+  d[0] = COMPLEX(-1.f, 0.5f);
+  auto best = std::make_shared<Reconstruction>(d.data(), (SUPPORTTYPE*)best_support,
+                                               std::array<std::size_t, 2>{(size_t)n, (size_t)n});
+  auto avg = std::make_shared<Reconstruction>(d.data(), sup.data(), std::array<std::size_t, 2>{(size_t)n, (size_t)n});
+  s.Crossover(recs, best, avg, crossbalance, 0.4f, crossexp, crossft, false, 0.f, true);
+  int used = 0;
+  for (int i = 0; i < count && i < (int)rc->records.size(); ++i) {
+    const ChildRecord& c = rc->records[i];
+    const int32_t v[11] = {c.p1, c.p2, c.p3, c.crossft, c.ssx, c.ssy, c.csx, c.csy, c.ox, c.oy, c.self};
+    std::memcpy(draws + 11 * i, v, sizeof v);
+    rot[i] = c.rot;
+    if (used + (int)c.cmap.size() > cmaps_cap) return -1;
+    std::memcpy(cmaps + used, c.cmap.data(), c.cmap.size() * sizeof(int32_t));
+    used += (int)c.cmap.size();
+  }
+  return (int)rc->records.size() == count ? used : -1;
+}
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+"""ctypes access to the reference's own host Solver built by build_ref.py
+(test infrastructure; available only where the reference checkout is)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import build_ref
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        path = build_ref.build()
+        if path is None:
+            return None
+        lib = C.CDLL(str(path))
+        lib.ref_prepare_pattern.restype = C.c_int
+        lib.ref_prepare_pattern.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        lib.ref_crossover_draws.restype = C.c_int
+        lib.ref_crossover_draws.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
+                                            C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        _lib = lib
+    return _lib
+
+
+def prepare_pattern(intensities, center=(-1, -1), use_bounds=True):
+    lib = load()
+    x = np.ascontiguousarray(intensities, dtype=np.float32)
+    out = np.empty_like(x)
+    lib.ref_prepare_pattern(x.ctypes.data, x.shape[0], int(center[0]), int(center[1]), int(bool(use_bounds)),
+                            out.ctypes.data)
+    return out
+
+
+def crossover_draws(n, errors, best_support, seed, crossbalance, crossexp=1.0, crossft=1.0):
+    """Returns (draws[count, 11] = p1, p2, p3, crossft, ssx, ssy, csx, csy, ox, oy, self; rot; crossmaps)."""
+    lib = load()
+    errors = np.ascontiguousarray(errors, dtype=np.float32)
+    best = np.ascontiguousarray(best_support, dtype=np.int32)
+    count = len(errors)
+    draws = np.empty((count, 11), np.int32)
+    rot = np.empty(count, np.float32)
+    cap = count * (n + 2) * (n + 2)
+    cm = np.empty(cap, np.int32)
+    used = lib.ref_crossover_draws(n, count, errors.ctypes.data, best.ctypes.data, int(seed), float(crossbalance),
+                                   float(crossexp), float(crossft), draws.ctypes.data, rot.ctypes.data,
+                                   cm.ctypes.data, cap)
+    if used < 0:
+        raise RuntimeError("reference crossover driver failed")
+    return draws, rot, cm[:used]

@@ -488,7 +488,8 @@ def prepare_pattern(intensities, center=(-1, -1), use_bounds=True):
     dd = np.where(inrange, d, 0)
     cand = inrange & (rp[dd] >= 0) & (pat < -0.5) & (pat > -1.5)
     bound = (rp[dd].astype(np.float64) + 1.0 * rstd[dd].astype(np.float64)).astype(np.float32)
-    newv = (-2.0 - np.sqrt(bound).astype(np.float32).astype(np.float64)).astype(np.float32)
+    with np.errstate(invalid="ignore"):  # non-candidate pixels may carry a negative bound
+        newv = (-2.0 - np.sqrt(bound).astype(np.float32).astype(np.float64)).astype(np.float32)
     pat = np.where(cand, newv, np.where(inrange, f32(-1.0), pat)).astype(np.float32)
     # ---- prepare
     out = np.empty_like(pat)
@@ -697,3 +698,38 @@ def new_individual(self_rho, self_S, p1, S1, p2, S2, p3, S3, avg_rho, A,
         out = ift(out)
     out = apply_support_er(out, s, real)
     return out, s
+
+
+def crossover_population(rhos, Ss, errors, best_S, avg_rho, A, rng, crossbalance, crossdiff, crossexp=1.0,
+                         crossftin=1.0, crosssym=False, use_average=0.0, update_support=True, real=0.0,
+                         minr=0.0, maxr=2.0):
+    """``Solver::Crossover`` (``solver.cpp:716-817``) with the per-child GPU
+    context steps (``gpu_context.cu:1468-1694, 2044-2117``) restated: order by
+    error, suppdim from the best support, average module of the best 66%,
+    draws, alignment of self / p2 / p3 / average to p1 (spectra not
+    normalised on this path), then the new individual.  Returns a list of
+    (density, support)."""
+    P = len(rhos)
+    N = np.asarray(rhos[0]).shape[-1]
+    order = sorted_indexes(errors)
+    suppdim = suppdim_of(best_S, N)
+    avg_mod = get_average_module(rhos, errors, True, 0.66)
+    draws = draw_crossover(rng, P, order, suppdim, N, crossbalance, crossexp, crossftin)
+    out = []
+    zeros = np.zeros((N, N), np.int32)
+    for i, d in enumerate(draws):
+        p1 = np.asarray(rhos[d.p1], dtype=np.complex128)
+
+        def align(x, s):
+            x = np.asarray(x, dtype=np.complex128)
+            sx, sy, sp, fl = get_shift(x, p1, A, minr, maxr, normalize_ft=False)
+            return shift(x, zeros if s is None else s, sx, sy, sp, fl)
+
+        r0, s0 = align(rhos[i], Ss[i])
+        r2, s2 = align(rhos[d.p2], Ss[d.p2])
+        r3, s3 = align(rhos[d.p3], Ss[d.p3])
+        ra, _ = align(avg_rho, None)
+        child, cs = new_individual(r0, s0, p1, Ss[d.p1], r2, s2, r3, s3, ra, A, avg_mod, d, crossdiff,
+                                   use_average, crosssym, real)
+        out.append((child, cs if update_support else np.asarray(Ss[i], np.int32)))
+    return out

