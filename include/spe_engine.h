@@ -196,6 +196,19 @@ int spe_crossover_draws(uint32_t seed, int count, const int32_t* order, float su
                         float crossexp, float crossft, int32_t* draws, float* rot, int32_t* cmaps, int cmaps_capacity,
                         int32_t* cmaps_used);
 
+/* Tile widths of the iteration kernels: columns per column-pass tile and
+ * rows per row-pass tile (<= 0: the built-in defaults).  Only widths
+ * compiled for the engine's pattern size are accepted. */
+int spe_set_tiles(spe_engine* e, int cols, int rows);
+int spe_get_tiles(spe_engine* e, int* cols, int* rows);
+
+/* Autotuner (no reference counterpart; the reference has fixed 32x32
+ * blocks, gpu_context.h:17-21): times every compiled tile width of the
+ * iteration kernels on the resident population [first, first+count) with
+ * `iterations` RAAR steps per trial, keeps the fastest and restores the
+ * densities.  cols / rows (may be NULL) receive the choice. */
+int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows);
+
 /* Waits for all work queued on the engine's stream. */
 int spe_synchronize(spe_engine* e);
 

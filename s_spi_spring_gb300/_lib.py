@@ -67,6 +67,9 @@ SIGNATURES = {
     "spe_average_module": (_i, [_vp, _i, _i, _fp, _i, _f, _fp]),
     "spe_crossover": (_i, [_vp, _i, _i, _fp, _i, _i, _i, _f, _f, _f, _f, _i, _f, _i, _f, _f, _f]),
     "spe_crossover_draws": (_i, [C.c_uint32, _i, _ip, _f, _i, _f, _f, _f, _ip, _fp, _ip, _i, _ip]),
+    "spe_set_tiles": (_i, [_vp, _i, _i]),
+    "spe_get_tiles": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
+    "spe_autotune": (_i, [_vp, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)]),
 }
 
 
@@ -212,6 +215,20 @@ class Engine:
 
     def synchronize(self):
         call("spe_synchronize", self.h)
+
+    # -- tuning ----------------------------------------------------------------
+    def set_tiles(self, cols=0, rows=0):
+        call("spe_set_tiles", self.h, int(cols), int(rows))
+
+    def tiles(self):
+        a, b = C.c_int(), C.c_int()
+        call("spe_get_tiles", self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def autotune(self, first, count, iterations=10):
+        a, b = C.c_int(), C.c_int()
+        call("spe_autotune", self.h, int(first), int(count), int(iterations), C.byref(a), C.byref(b))
+        return a.value, b.value
 
     # -- population-level operations --------------------------------------------
     def seed(self, seed: int):

@@ -275,7 +275,8 @@ int do_iterate(spe_engine* e, int first, int count, int upd, int iters, float be
   if (count == 0) return SPE_OK;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   const spe::Gate g = (upd == 1) ? gate_raar(real) : gate_er(real);
-  CK(e->ops->iterate(make_ctx(e, first, count), upd, iters, beta, g), "iteration kernels");
+  CK(e->ops->iterate(make_ctx(e, first, count), upd, iters, beta, g, e->tile_cols, e->tile_rows),
+     "iteration kernels");
   return SPE_OK;
 }
 
@@ -593,6 +594,96 @@ int spe_sequence(spe_engine* e, int first, int count, const spe_op* ops, int nop
     }
   }
   if (metrics) return spe_evaluate(e, first, count, reality, realpen, metrics);
+  return SPE_OK;
+}
+
+int spe_set_tiles(spe_engine* e, int cols, int rows) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  int w[8];
+  auto ok = [&](int v, int (*f)(int*)) {
+    if (v <= 0) return true;
+    const int k = f(w);
+    for (int i = 0; i < k; ++i)
+      if (w[i] == v) return true;
+    return false;
+  };
+  if (!ok(cols, e->ops->col_widths) || !ok(rows, e->ops->row_widths))
+    return fail(SPE_ERR_INVALID, "tile widths %d/%d not compiled for size %d", cols, rows, e->n);
+  e->tile_cols = cols;
+  e->tile_rows = rows;
+  return SPE_OK;
+}
+
+int spe_get_tiles(spe_engine* e, int* cols, int* rows) {
+  if (!e || !cols || !rows) return fail(SPE_ERR_INVALID, "null argument");
+  *cols = e->tile_cols > 0 ? e->tile_cols : e->ops->default_cols;
+  *rows = e->tile_rows > 0 ? e->tile_rows : e->ops->default_rows;
+  return SPE_OK;
+}
+
+// Times the compiled tile widths of the iteration kernels on the resident
+// population [first, first+count) (RAAR, `iterations` per trial, median of
+// three) -- first the column pass with the current row width, then the row
+// pass -- keeps the fastest and restores the densities.
+int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if ((rc = need_amp(e))) return rc;
+  if (count <= 0 || iterations <= 0) return fail(SPE_ERR_INVALID, "autotune needs individuals and iterations");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  const size_t bytes = (size_t)count * e->npix * sizeof(float2);
+  float2* save = e->T2 + (size_t)first * e->npix;
+  CK(cudaMemcpyAsync(save, e->rho + (size_t)first * e->npix, bytes, cudaMemcpyDeviceToDevice, e->st), "save");
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a), "event");
+  CK(cudaEventCreate(&b), "event");
+  const spe::Gate g = gate_raar(0.f);
+  spe::Ctx c = make_ctx(e, first, count);
+  auto trial = [&](int wc, int wr, float* ms) -> int {
+    float t[3];
+    for (int r = 0; r < 3; ++r) {
+      CK(cudaMemcpyAsync(e->rho + (size_t)first * e->npix, save, bytes, cudaMemcpyDeviceToDevice, e->st), "restore");
+      CK(cudaEventRecord(a, e->st), "event");
+      CK(e->ops->iterate(c, 1, iterations, 0.87f, g, wc, wr), "autotune iteration");
+      CK(cudaEventRecord(b, e->st), "event");
+      CK(cudaEventSynchronize(b), "event");
+      CK(cudaEventElapsedTime(&t[r], a, b), "event");
+    }
+    std::sort(t, t + 3);
+    *ms = t[1];
+    return SPE_OK;
+  };
+  int wcs[8], wrs[8];
+  const int nc = e->ops->col_widths(wcs), nr = e->ops->row_widths(wrs);
+  int best_c = e->tile_cols > 0 ? e->tile_cols : e->ops->default_cols;
+  int best_r = e->tile_rows > 0 ? e->tile_rows : e->ops->default_rows;
+  float best = 1e30f;
+  for (int i = 0; i < nc; ++i) {
+    float ms;
+    if ((rc = trial(wcs[i], best_r, &ms))) break;
+    if (ms < best) {
+      best = ms;
+      best_c = wcs[i];
+    }
+  }
+  best = 1e30f;
+  for (int i = 0; !rc && i < nr; ++i) {
+    float ms;
+    if ((rc = trial(best_c, wrs[i], &ms))) break;
+    if (ms < best) {
+      best = ms;
+      best_r = wrs[i];
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(e->rho + (size_t)first * e->npix, save, bytes, cudaMemcpyDeviceToDevice, e->st), "restore");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  e->tile_cols = best_c;
+  e->tile_rows = best_r;
+  if (cols) *cols = best_c;
+  if (rows) *rows = best_r;
   return SPE_OK;
 }
 

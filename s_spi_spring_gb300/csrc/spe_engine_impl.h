@@ -37,6 +37,7 @@ struct spe_engine {
   float2* ref = nullptr;       // reference density of an alignment, n*n
   void* work = nullptr;        // grow-only scratch of the population ops
   size_t work_bytes = 0;
+  int tile_cols = 0, tile_rows = 0;  // iteration kernel tile widths (0: defaults)
 };
 
 

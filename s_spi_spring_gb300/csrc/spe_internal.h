@@ -58,8 +58,9 @@ struct SizeOps {
   int tiles_cols;  // CTAs per individual of a column pass
   int tw_size;     // twiddle table entries
   void (*fill_tw)(float2*);
-  // upd: 0 HIO, 1 RAAR, 2 ER
-  cudaError_t (*iterate)(const Ctx&, int upd, int iterations, float beta, Gate g);
+  // upd: 0 HIO, 1 RAAR, 2 ER; wc / wr: tile widths of the column / row
+  // pass of the iteration kernels (<= 0: defaults)
+  cudaError_t (*iterate)(const Ctx&, int upd, int iterations, float beta, Gate g, int wc, int wr);
   // blurred modulus into M, per-CTA max into partials
   cudaError_t (*blur_magnitude)(const Ctx&, float sigma_ft);
   // error terms: stage 1 -> partials (modulesum), stage 2 -> partials+P1
@@ -82,6 +83,10 @@ struct SizeOps {
   cudaError_t (*corr_peak_idx)(const Ctx&, const float2* D, const float2* Dref, const int* xi, const int* ri,
                                int sign, float minr, float maxr, int norm_d, int norm_ref, float2* scratch,
                                double* partials);
+  // tile widths compiled for this size
+  int (*col_widths)(int* out);
+  int (*row_widths)(int* out);
+  int default_cols, default_rows;
 };
 
 const SizeOps* size_ops(int n);

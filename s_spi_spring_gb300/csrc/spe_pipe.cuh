@@ -22,44 +22,50 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 // Column exchange layout that keeps the element pairs of a 16-byte copy
-// adjacent.  W = 16: plain rows of 128 bytes (a warp covers whole rows).
-// W <= 8: rows of W*8 bytes; rows l and l^1 swap when bit 3 of l is set, so
-// the four rows a warp touches in a Stockham store (l = 8j+q) alternate
-// between the two 64-byte halves of the bank array.
+// adjacent (columns are never permuted, only rows).  W = 16: plain rows of
+// 128 bytes (a warp covers whole rows).  W = 8 / 4: rows of 64 / 32 bytes;
+// row l moves to l ^ ((l >> 3) & (16/W - 1)), so the rows a warp touches in
+// a Stockham store (l = 8j+q, consecutive j) fall into different bank groups.
 template <int L, int W>
 struct LayCol {
   static constexpr int SIZE = L * W;
   static __device__ __forceinline__ int idx(int l, int c) {
     if (W >= 16) return l * W + c;
-    return (l ^ ((l >> 3) & 1)) * W + c;
+    return (l ^ ((l >> 3) & (16 / W - 1))) * W + c;
   }
 };
 
 constexpr int align128(int b) { return (b + 127) & ~127; }
 
-template <int N>
-struct PipeCfg {
+template <int N, int W>
+struct ColCfg {  // column pass with W columns per tile
   static constexpr int TPT = Plan<N>::TPT;
   static constexpr int E = Elems<N>::value;
   static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
-  // column pass
-  static constexpr int WC = (N >= 2048) ? 4 : (N >= 512 ? 8 : 16);
-  static constexpr int NTC = WC * TPT;
-  static constexpr int C_T = align128(N * WC * 8);
-  static constexpr int C_A = align128(N * WC * 4);
-  static constexpr int C_STAGE = C_T + C_A;
-  static constexpr size_t C_SMEM = (size_t)TWB + 2 * C_STAGE;
-  // row pass
-  static constexpr int WR = (N <= 256) ? 8 : (N == 384 ? 8 : (N <= 512 ? 4 : (N <= 1024 ? 2 : 1)));
-  static constexpr int NTR = WR * TPT;
+  static constexpr int NT = W * TPT;
+  static constexpr int C_T = align128(N * W * 8);
+  static constexpr int C_A = align128(N * W * 4);
+  static constexpr int STAGE = C_T + C_A;
+  static constexpr size_t SMEM = (size_t)TWB + 2 * STAGE;
+  // two CTAs per SM when the registers of E elements per thread allow it
+  static constexpr int MINB = (E <= 8 && NT <= 512) ? 2 : 1;
+};
+
+template <int N, int W>
+struct RowCfg {  // row pass with W rows per tile
+  static constexpr int TPT = Plan<N>::TPT;
+  static constexpr int E = Elems<N>::value;
+  static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
+  static constexpr int NT = W * TPT;
   // (the padded exchange layout is not 16-byte aligned per element pair, so
   // the row stage holds T plainly and the exchanges use their own buffer)
-  static constexpr int R_T = align128(N * WR * 8);
-  static constexpr int R_R = align128(N * WR * 8);
-  static constexpr int R_S = align128(N * WR * 4);
-  static constexpr int R_STAGE = R_T + R_R + R_S;
-  static constexpr int R_X = align128(LayPad<N, WR>::SIZE * 8);
-  static constexpr size_t R_SMEM = (size_t)TWB + R_X + 2 * R_STAGE;
+  static constexpr int R_T = align128(N * W * 8);
+  static constexpr int R_R = align128(N * W * 8);
+  static constexpr int R_S = align128(N * W * 4);
+  static constexpr int STAGE = R_T + R_R + R_S;
+  static constexpr int R_X = align128(LayPad<N, W>::SIZE * 8);
+  static constexpr size_t SMEM = (size_t)TWB + R_X + 2 * STAGE;
+  static constexpr int MINB = (NT <= 256 || (E <= 8 && NT <= 512)) ? 2 : 1;
 };
 
 template <int N>
@@ -69,12 +75,12 @@ __device__ __forceinline__ void load_twiddles(float2* tw, const float2* __restri
 }
 
 // column pass: T -> FFT+ (y) -> P_M with A -> FFT- (y) -> T
-template <int N>
-__global__ void __launch_bounds__(PipeCfg<N>::NTC, 2)
+template <int N, int W>
+__global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
     k_cols_project(float2* __restrict__ T, const float* __restrict__ A, int first, int count,
                    const float2* __restrict__ twg) {
-  using C = PipeCfg<N>;
-  constexpr int W = C::WC, NT = C::NTC, E = C::E, TPI = N / W;
+  using C = ColCfg<N, W>;
+  constexpr int NT = C::NT, E = C::E, TPI = N / W;
   using Lay = LayCol<N, W>;
   extern __shared__ __align__(128) unsigned char sm[];
   float2* tw = reinterpret_cast<float2*>(sm);
@@ -87,8 +93,8 @@ __global__ void __launch_bounds__(PipeCfg<N>::NTC, 2)
   auto stage_tile = [&](int tile, int s) {
     const int p = first + tile / TPI;
     const int x0 = (tile % TPI) * W;
-    float2* sT = reinterpret_cast<float2*>(stages + s * C::C_STAGE);
-    float* sA = reinterpret_cast<float*>(stages + s * C::C_STAGE + C::C_T);
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::STAGE);
+    float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
     const float2* gT = T + (size_t)p * N * N + x0;
     for (int q = t; q < N * W / 2; q += NT) {
       const int y = q / (W / 2), h = q - y * (W / 2);
@@ -110,8 +116,8 @@ __global__ void __launch_bounds__(PipeCfg<N>::NTC, 2)
     cp_async_wait_prev();
     __syncthreads();
     const int s = k & 1;
-    float2* sT = reinterpret_cast<float2*>(stages + s * C::C_STAGE);
-    const float* sA = reinterpret_cast<const float*>(stages + s * C::C_STAGE + C::C_T);
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::STAGE);
+    const float* sA = reinterpret_cast<const float*>(stages + s * C::STAGE + C::C_T);
     const int p = first + tile / TPI;
     const int x = (tile % TPI) * W + c;
     float2 v[E];
@@ -133,12 +139,12 @@ __global__ void __launch_bounds__(PipeCfg<N>::NTC, 2)
 }
 
 // row pass: T -> FFT- (x) -> /N^2 -> update with (rho, S) -> rho -> FFT+ (x) -> T
-template <int N, int UPD>
-__global__ void __launch_bounds__(PipeCfg<N>::NTR, 2)
+template <int N, int W, int UPD>
+__global__ void __launch_bounds__(RowCfg<N, W>::NT, RowCfg<N, W>::MINB)
     k_rows_iterate(float2* __restrict__ T, float2* __restrict__ rho, const int* __restrict__ S, int first,
                    int count, float scale, float beta, Gate g, const float2* __restrict__ twg) {
-  using C = PipeCfg<N>;
-  constexpr int W = C::WR, NT = C::NTR, E = C::E, TPT = C::TPT, TPI = N / W;
+  using C = RowCfg<N, W>;
+  constexpr int NT = C::NT, E = C::E, TPT = C::TPT, TPI = N / W;
   using Lay = LayPad<N, W>;
   extern __shared__ __align__(128) unsigned char sm[];
   float2* tw = reinterpret_cast<float2*>(sm);
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(PipeCfg<N>::NTR, 2)
     const int p = first + tile / TPI;
     const int y0 = (tile % TPI) * W;
     const size_t base = (size_t)p * N * N + (size_t)y0 * N;
-    unsigned char* st = stages + s * C::R_STAGE;
+    unsigned char* st = stages + s * C::STAGE;
     float2* sT = reinterpret_cast<float2*>(st);
     float2* sR = reinterpret_cast<float2*>(st + C::R_T);
     int* sS = reinterpret_cast<int*>(st + C::R_T + C::R_R);
@@ -176,7 +182,7 @@ __global__ void __launch_bounds__(PipeCfg<N>::NTR, 2)
     cp_async_wait_prev();
     __syncthreads();
     const int s = k & 1;
-    unsigned char* st = stages + s * C::R_STAGE;
+    unsigned char* st = stages + s * C::STAGE;
     const float2* sT = reinterpret_cast<const float2*>(st);
     const float2* sR = reinterpret_cast<const float2*>(st + C::R_T);
     const int* sS = reinterpret_cast<const int*>(st + C::R_T + C::R_R);

@@ -60,30 +60,77 @@ cudaError_t configure(K kern, size_t smem, unsigned long long& configured) {
   return cudaSuccess;
 }
 
+// tile-width variants compiled per size: those whose tile fits in shared
+// memory with whole warps
+constexpr size_t kMaxSmem = 232448;  // 227 KB per CTA
+template <int N, int W>
+constexpr bool col_ok() {
+  return W <= N && N % W == 0 && ColCfg<N, W>::NT % 32 == 0 && ColCfg<N, W>::NT <= 1024 &&
+         ColCfg<N, W>::SMEM <= kMaxSmem;
+}
+template <int N, int W>
+constexpr bool row_ok() {
+  return W <= N && N % W == 0 && RowCfg<N, W>::NT % 32 == 0 && RowCfg<N, W>::NT <= 1024 &&
+         RowCfg<N, W>::SMEM <= kMaxSmem;
+}
+constexpr int kColWidths[3] = {4, 8, 16};
+constexpr int kRowWidths[5] = {1, 2, 4, 8, 16};
+
+// default widths (before any tuning)
 template <int N>
+struct DefaultTiles {
+  static constexpr int cols = (N >= 2048) ? 4 : (N >= 512 ? 8 : 16);
+  static constexpr int rows = (N <= 256) ? 8 : (N == 384 ? 8 : (N <= 512 ? 4 : (N <= 1024 ? 2 : 1)));
+};
+
+template <int N, int W>
 cudaError_t launch_cols_project(const Ctx& c) {
-  using P = PipeCfg<N>;
-  auto kern = k_cols_project<N>;
+  using P = ColCfg<N, W>;
+  auto kern = k_cols_project<N, W>;
   static unsigned long long configured = 0ull;
-  cudaError_t e = configure(kern, P::C_SMEM, configured);
+  cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
-  const int tiles = c.count * (N / P::WC);
+  const int tiles = c.count * (N / W);
   const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-  kern<<<grid, P::NTC, P::C_SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
+  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
   return cudaGetLastError();
 }
 
-template <int N, int UPD>
+template <int N, int W, int UPD>
 cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
-  using P = PipeCfg<N>;
-  auto kern = k_rows_iterate<N, UPD>;
+  using P = RowCfg<N, W>;
+  auto kern = k_rows_iterate<N, W, UPD>;
   static unsigned long long configured = 0ull;
-  cudaError_t e = configure(kern, P::R_SMEM, configured);
+  cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
-  const int tiles = c.count * (N / P::WR);
+  const int tiles = c.count * (N / W);
   const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-  kern<<<grid, P::NTR, P::R_SMEM, c.st>>>(c.T, c.rho, c.S, c.first, c.count, scale, beta, g, c.tw);
+  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.rho, c.S, c.first, c.count, scale, beta, g, c.tw);
   return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_cols_w(const Ctx& c, int w) {
+  switch (w) {
+    case 4: if constexpr (col_ok<N, 4>()) return launch_cols_project<N, 4>(c); break;
+    case 8: if constexpr (col_ok<N, 8>()) return launch_cols_project<N, 8>(c); break;
+    case 16: if constexpr (col_ok<N, 16>()) return launch_cols_project<N, 16>(c); break;
+    default: break;
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int N, int UPD>
+cudaError_t launch_rows_w(const Ctx& c, int w, float scale, float beta, Gate g) {
+  switch (w) {
+    case 1: if constexpr (row_ok<N, 1>()) return launch_rows_iterate<N, 1, UPD>(c, scale, beta, g); break;
+    case 2: if constexpr (row_ok<N, 2>()) return launch_rows_iterate<N, 2, UPD>(c, scale, beta, g); break;
+    case 4: if constexpr (row_ok<N, 4>()) return launch_rows_iterate<N, 4, UPD>(c, scale, beta, g); break;
+    case 8: if constexpr (row_ok<N, 8>()) return launch_rows_iterate<N, 8, UPD>(c, scale, beta, g); break;
+    case 16: if constexpr (row_ok<N, 16>()) return launch_rows_iterate<N, 16, UPD>(c, scale, beta, g); break;
+    default: break;
+  }
+  return cudaErrorInvalidValue;
 }
 
 #define SPE_TRY(x)                         \
@@ -119,7 +166,7 @@ struct SizeImpl {
   }
 
   template <int UPD>
-  static cudaError_t iterate_t(const Ctx& c, int iters, float beta, Gate g) {
+  static cudaError_t iterate_t(const Ctx& c, int iters, float beta, Gate g, int wc, int wr) {
     SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(c, c.rho, c.T, g, nullptr), c.count, c.st, c.tw)));
     const OpColsProject proj = cols_project(c);
     OpRowsIterate<UPD> it;
@@ -132,10 +179,10 @@ struct SizeImpl {
     it.beta = beta;
     it.g = g;
     for (int i = 0; i < iters; ++i) {
-      SPE_TRY(launch_cols_project<N>(c));
-      SPE_TRY((launch_rows_iterate<N, UPD>(c, scale(), beta, g)));
+      SPE_TRY(launch_cols_w<N>(c, wc));
+      SPE_TRY((launch_rows_w<N, UPD>(c, wr, scale(), beta, g)));
     }
-    SPE_TRY(launch_cols_project<N>(c));
+    SPE_TRY(launch_cols_w<N>(c, wc));
     OpRowsFinal fin;
     fin.first = c.first;
     fin.partials = nullptr;
@@ -145,12 +192,32 @@ struct SizeImpl {
     return launch_pass<N, AX_ROWS>(fin, c.count, c.st, c.tw);
   }
 
-  static cudaError_t iterate(const Ctx& c, int upd, int iters, float beta, Gate g) {
+  // wc / wr: tile widths of the column / row pass (<= 0: defaults)
+  static cudaError_t iterate(const Ctx& c, int upd, int iters, float beta, Gate g, int wc, int wr) {
+    if (wc <= 0) wc = DefaultTiles<N>::cols;
+    if (wr <= 0) wr = DefaultTiles<N>::rows;
     switch (upd) {
-      case 0: return iterate_t<UPD_HIO>(c, iters, beta, g);
-      case 1: return iterate_t<UPD_RAAR>(c, iters, beta, g);
-      default: return iterate_t<UPD_ER>(c, iters, beta, g);
+      case 0: return iterate_t<UPD_HIO>(c, iters, beta, g, wc, wr);
+      case 1: return iterate_t<UPD_RAAR>(c, iters, beta, g, wc, wr);
+      default: return iterate_t<UPD_ER>(c, iters, beta, g, wc, wr);
     }
+  }
+
+  static int col_widths(int* out) {
+    int k = 0;
+    if constexpr (col_ok<N, 4>()) out[k++] = 4;
+    if constexpr (col_ok<N, 8>()) out[k++] = 8;
+    if constexpr (col_ok<N, 16>()) out[k++] = 16;
+    return k;
+  }
+  static int row_widths(int* out) {
+    int k = 0;
+    if constexpr (row_ok<N, 1>()) out[k++] = 1;
+    if constexpr (row_ok<N, 2>()) out[k++] = 2;
+    if constexpr (row_ok<N, 4>()) out[k++] = 4;
+    if constexpr (row_ok<N, 8>()) out[k++] = 8;
+    if constexpr (row_ok<N, 16>()) out[k++] = 16;
+    return k;
   }
 
   static cudaError_t blur_magnitude(const Ctx& c, float sigma_ft) {
@@ -344,7 +411,11 @@ struct SizeImpl {
                               &SizeImpl<N>::fft2,
                               &SizeImpl<N>::ft_magnitude,
                               &SizeImpl<N>::abs_spectrum_items,
-                              &SizeImpl<N>::corr_peak_idx};
+                              &SizeImpl<N>::corr_peak_idx,
+                              &SizeImpl<N>::col_widths,
+                              &SizeImpl<N>::row_widths,
+                              DefaultTiles<N>::cols,
+                              DefaultTiles<N>::rows};
     return &t;
   }
 };
