@@ -209,6 +209,24 @@ int spe_get_tiles(spe_engine* e, int* cols, int* rows);
  * densities.  cols / rows (may be NULL) receive the choice. */
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows);
 
+/* Allocation-free HIO / RAAR / ER (no counterpart in the reference).
+ * For callers that may not allocate GPU memory while they run -- e.g. an
+ * online analysis step inside a detector pipeline that reserves the whole
+ * device at start-up, or code that must not let cudaMalloc synchronise the
+ * device.  Same arithmetic as spe_hio / spe_raar / spe_er, but on device
+ * arrays the caller owns: density (count*n*n complex64, updated in place),
+ * support (count*n*n int32), amplitudes (n*n float, the output of
+ * spe_prepare_pattern); algorithm is SPE_OP_HIO, SPE_OP_RAAR or SPE_OP_ER;
+ * work is queued on cuda_stream (a cudaStream_t, NULL: the legacy stream).
+ * The scratch lives in a 16 MiB file-scope device array that every GPU
+ * using the library keeps until exit; calls needing more (count*n*n*8 bytes)
+ * are rejected with SPE_ERR_INVALID.  The first call on a device sets up
+ * that array's address and the twiddle tables (synchronously), so make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (e.g. on two streams) race.  No memory is allocated. */
+int spe_iterate_noalloc(int n, void* density, const int32_t* support, const float* amplitudes, int count,
+                        int algorithm, int iterations, float beta, float reality, void* cuda_stream);
+
 /* Waits for all work queued on the engine's stream. */
 int spe_synchronize(spe_engine* e);
 

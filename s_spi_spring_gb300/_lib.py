@@ -70,6 +70,7 @@ SIGNATURES = {
     "spe_set_tiles": (_i, [_vp, _i, _i]),
     "spe_get_tiles": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
     "spe_autotune": (_i, [_vp, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)]),
+    "spe_iterate_noalloc": (_i, [_i, _vp, _vp, _vp, _i, _i, _i, _f, _f, _vp]),
 }
 
 
