@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths")
     return ap.parse_args()
 
 
@@ -192,6 +195,7 @@ def run_engine(args):
     stream = torch.cuda.Stream(device=local)
     eng.set_stream(stream.cuda_stream)
     eng.upload(0, dens, S)
+    tiles = eng.tiles() if args.no_tune else eng.autotune(0, POP, 10)
     eng.synchronize()
 
     def barrier():
@@ -286,7 +290,8 @@ def run_engine(args):
         "config": {"workload": "memetic population RAAR: 512x512 complex64, population 64, beta 0.87, "
                                f"{args.iters} iterations per step",
                    "pattern": N, "population": POP, "iterations_per_step": args.iters,
-                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (320 MiB working set)"},
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (320 MiB working set)",
+                   "tiles": {"cols": tiles[0], "rows": tiles[1], "autotuned": not args.no_tune}},
         "e2e": {"value": round(e2e_value, 1), "unit": "iter*individuals/s",
                 "h2d_bytes_per_step": int(h_dens.numel() * 4 + h_supp.numel() * 4),
                 "d2h_bytes_per_step": int(h_out.numel() * 4)},
@@ -355,8 +360,26 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_profile_case(args):
+    """One RAAR call on the resident workload (for ncu captures)."""
+    from s_spi_spring_gb300 import _lib
+    A, dens, S = workload()
+    eng = _lib.Engine(N, 0)
+    eng.set_amplitudes(A)
+    eng.upload(0, dens, S)
+    if not args.no_tune:
+        eng.autotune(0, POP, 4)
+    eng.raar(0, POP, 1, BETA, 0.0)  # warm-up
+    eng.raar(0, POP, args.profile_iters, BETA, 0.0)
+    eng.synchronize()
+    print(json.dumps({"profile_case": "RAAR", "iterations": args.profile_iters, "tiles": eng.tiles()}))
+
+
 def main():
     args = parse()
+    if args.profile_iters > 0:
+        run_profile_case(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

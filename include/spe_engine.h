@@ -186,6 +186,24 @@ int spe_crossover(spe_engine* e, int first, int count, const float* errors, int 
                   int dst_first, float crossbalance, float crossdiff, float crossexp, float crossft, int crosssym,
                   float use_average, int update_support, float reality, float minr, float maxr);
 
+/* Solver::Initialize_pop (src/solver.cpp:824-957): `count` starting
+ * individuals into [first, first+count): a centred disc support of diameter
+ * support_size; inside it a sum of nitems in [nitems_min, nitems_max]
+ * disc profiles (diameters in [itemsize_min, itemsize_max], phases within
+ * +-phaserange*pi), modulus raised to an exponent in
+ * [exponent_min, exponent_max], scaled to the pattern's power on the known
+ * pixels times a factor in [scaling_min, scaling_max].  Draws come from the
+ * engine's generator (spe_seed) in the reference's order.  suppcut is
+ * accepted and unused, as in the reference. */
+int spe_initialize_pop(spe_engine* e, int first, int count, int support_size, float itemsize_min, float itemsize_max,
+                       int nitems_min, int nitems_max, float exponent_min, float exponent_max, float scaling_min,
+                       float scaling_max, float phaserange, float suppcut);
+
+/* Copies `count` individuals (density and support) between population
+ * slots (the selection step of spring/mpr.py:341-347 on the device).
+ * Overlapping source and destination ranges are rejected. */
+int spe_copy(spe_engine* e, int src, int dst, int count);
+
 /* Host-only: the random draws of Solver::Crossover (src/solver.cpp:750-801)
  * for `count` children from std::mt19937(seed), given the error order and
  * suppdim.  draws: count*11 ints (p1, p2, p3, crossft, squaresizex,

@@ -11,7 +11,12 @@
 //     Context (this file's own class, not reference code) is installed in
 //     place of the GPU contexts; it identifies the parents passed to
 //     set_parents_density by a marker value each individual carries and
-//     records the arguments of get_new_individual.
+//     records the arguments of get_new_individual;
+//   * Solver::Initialize_pop (src/solver.cpp:822-957): every draw, the disc
+//     profiles and the scaling, with a context whose transform is a
+//     double-precision DFT.
+#include <cmath>
+#include <complex>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -61,9 +66,62 @@ class RecordingContext : public Context {
   std::vector<ChildRecord> records;
 };
 
+// Context with a working transform, for Solver::Initialize_pop: set_density
+// / get_ft / get_density (the reference's get_ft is the unnormalised
+// exponent +i transform, gpu_context.cu:748-754), here a double-precision
+// separable DFT -- fine at the small sizes the fixtures use.
+class TransformContext : public Context {
+ public:
+  TransformContext(int n, int seed) : Context(n, seed), density((size_t)n * n) {}
+  void set_density(COMPLEX* d) override { std::memcpy(density.data(), d, density.size() * sizeof(COMPLEX)); }
+  void get_density(COMPLEX* d) override { std::memcpy(d, density.data(), density.size() * sizeof(COMPLEX)); }
+  void get_ft() override {
+    const int n = npixels;
+    std::vector<std::complex<double>> a(density.begin(), density.end()), b((size_t)n * n);
+    std::vector<std::complex<double>> w(n);
+    for (int k = 0; k < n; ++k) w[k] = std::polar(1.0, 2.0 * M_PI * k / n);
+    for (int y = 0; y < n; ++y)  // along x
+      for (int k = 0; k < n; ++k) {
+        std::complex<double> acc = 0;
+        for (int x = 0; x < n; ++x) acc += a[(size_t)y * n + x] * w[((size_t)k * x) % n];
+        b[(size_t)y * n + k] = acc;
+      }
+    for (int x = 0; x < n; ++x)  // along y
+      for (int k = 0; k < n; ++k) {
+        std::complex<double> acc = 0;
+        for (int y = 0; y < n; ++y) acc += b[(size_t)y * n + x] * w[((size_t)k * y) % n];
+        a[(size_t)k * n + x] = acc;
+      }
+    for (size_t i = 0; i < a.size(); ++i) density[i] = COMPLEX((FLOAT)a[i].real(), (FLOAT)a[i].imag());
+  }
+  std::vector<COMPLEX> density;
+};
+
 }  // namespace
 
 extern "C" {
+
+// Solver::Initialize_pop on the CPU with one transform context seeded like
+// the reference's first context.  density_out: count*n*n complex64,
+// support_out: count*n*n int32.
+int ref_initialize_pop(const float* intensities, int n, int count, int support_size, float isz0, float isz1, int ni0,
+                       int ni1, float e0, float e1, float s0, float s1, float phase, int seed, float* density_out,
+                       int32_t* support_out) {
+  std::vector<FLOAT> pat(intensities, intensities + (size_t)n * n);
+  Solver s(pat.data(), {(size_t)n, (size_t)n}, {-1, -1}, 0, 0, 1, false, std::vector<int>{}, seed);
+  for (auto* c : s.contexts) delete c;
+  s.contexts.clear();
+  s.contexts.push_back(new TransformContext(n, 1 * seed));
+  s.nthreads = 1;
+  auto recs = s.Initialize_pop(count, support_size, {isz0, isz1}, {ni0, ni1}, {e0, e1}, {s0, s1}, phase, 0.f);
+  const size_t np = (size_t)n * n;
+  for (int k = 0; k < count; ++k) {
+    std::memcpy(density_out + 2 * np * k, recs[k]->density.data(), np * sizeof(COMPLEX));
+    std::memcpy(support_out + np * k, recs[k]->support.data(), np * sizeof(SUPPORTTYPE));
+  }
+  return 0;
+}
+
 
 // Solver(pattern, center, ...) -> Solver::pattern (the encoded amplitudes)
 int ref_prepare_pattern(const float* intensities, int n, int cx, int cy, int use_bounds, float* out) {

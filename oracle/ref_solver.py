@@ -23,6 +23,10 @@ def load():
         lib.ref_crossover_draws.restype = C.c_int
         lib.ref_crossover_draws.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
                                             C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        lib.ref_initialize_pop.restype = C.c_int
+        lib.ref_initialize_pop.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
+                                           C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
+                                           C.c_void_p, C.c_void_p]
         _lib = lib
     return _lib
 
@@ -52,3 +56,17 @@ def crossover_draws(n, errors, best_support, seed, crossbalance, crossexp=1.0, c
     if used < 0:
         raise RuntimeError("reference crossover driver failed")
     return draws, rot, cm[:used]
+
+
+def initialize_pop(intensities, count, support_size, itemsize, nitems, exponent, scaling, phase, seed):
+    """The reference's Solver::Initialize_pop (use_bounds off) on the CPU."""
+    lib = load()
+    I = np.ascontiguousarray(intensities, dtype=np.float32)
+    n = I.shape[0]
+    d = np.empty((count, n, n), np.complex64)
+    s = np.empty((count, n, n), np.int32)
+    lib.ref_initialize_pop(I.ctypes.data, n, count, support_size, float(itemsize[0]), float(itemsize[1]),
+                           int(nitems[0]), int(nitems[1]), float(exponent[0]), float(exponent[1]),
+                           float(scaling[0]), float(scaling[1]), float(phase), int(seed), d.ctypes.data,
+                           s.ctypes.data)
+    return d, s

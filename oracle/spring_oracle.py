@@ -733,3 +733,54 @@ def crossover_population(rhos, Ss, errors, best_S, avg_rho, A, rng, crossbalance
                                    use_average, crosssym, real)
         out.append((child, cs if update_support else np.asarray(Ss[i], np.int32)))
     return out
+
+
+# ----------------------------------------------------------------------------
+# Starting population (Solver::Initialize_rec, ``solver.cpp:880-957``)
+# ----------------------------------------------------------------------------
+def initialize_pop(A, rng, count, support_size, itemsize, nitems, exponent, scaling, phase):
+    """Restates ``Solver::Initialize_pop`` with one context: per individual the
+    draws (``:882-906``) in the reference's order and float arithmetic, the
+    disc support of diameter ``support_size`` centred in the field, the sum of
+    disc profiles with phases, the modulus exponent, and the scaling to the
+    pattern's power over the known pixels (``:938-950``)."""
+    f32 = np.float32
+    A = np.asarray(A, dtype=np.float32)
+    N = A.shape[0]
+    ss = int(support_size)
+    dens = np.zeros((count, N, N), np.complex64)
+    supp = np.zeros((count, N, N), np.int32)
+    iy, ix = np.mgrid[0:ss, 0:ss]
+    supprad = np.sqrt((ix - ss / 2.0) ** 2 + (iy - ss / 2.0) ** 2)
+    inside = supprad <= ss / 2.0
+    off = N // 2 - ss // 2
+    known = A >= 0
+    for k in range(count):
+        nit = int(rng.rand(nitems[0], float(nitems[1]) + 0.99))
+        ex = rng.rand(exponent[0], exponent[1])
+        sc = rng.rand(scaling[0], scaling[1])
+        items = []
+        for _ in range(nit):
+            sigma = f32(np.sqrt(rng.rand(float(itemsize[0]) ** 2, float(itemsize[1]) ** 2)) / 2.0)
+            cx = rng.rand(sigma, f32(ss - sigma))
+            cy = rng.rand(sigma, f32(ss - sigma))
+            ph = rng.rand(-phase * M_PI, phase * M_PI)
+            items.append((sigma, cx, cy, ph))
+        box = np.zeros((ss, ss), np.complex64)
+        for sigma, cx, cy, ph in items:
+            rad = np.sqrt(((ix - cx) ** 2 + (iy - cy) ** 2).astype(np.float32)).astype(np.float32)
+            on = inside & (rad < sigma)
+            with np.errstate(invalid="ignore"):
+                val = (2.0 * float(sigma) * np.sin(np.arccos(rad / sigma)).astype(np.float32)).astype(np.float32)
+            box[on] += (val[on] * np.cos(f32(ph)) + 1j * val[on] * np.sin(f32(ph))).astype(np.complex64)
+        mod = np.abs(box).astype(np.float32)
+        nz = inside & (mod > 0)
+        box[nz] = (box[nz] / mod[nz] * np.power(mod[nz], f32(ex))).astype(np.complex64)
+        box[~inside] = 0
+        dens[k, off:off + ss, off:off + ss] = box
+        supp[k, off:off + ss, off:off + ss] = inside.astype(np.int32)
+        F = ft(dens[k].astype(np.complex128))
+        norm = np.sum(np.abs(F[known]) ** 2)
+        norm_new = np.sum(A[known].astype(np.float64) ** 2)
+        dens[k] = (dens[k] * f32(np.sqrt(f32(norm_new) / f32(norm)) * sc)).astype(np.complex64)
+    return dens, supp

@@ -71,6 +71,8 @@ SIGNATURES = {
     "spe_get_tiles": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
     "spe_autotune": (_i, [_vp, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)]),
     "spe_iterate_noalloc": (_i, [_i, _vp, _vp, _vp, _i, _i, _i, _f, _f, _vp]),
+    "spe_initialize_pop": (_i, [_vp, _i, _i, _i, _f, _f, _i, _i, _f, _f, _f, _f, _f, _f]),
+    "spe_copy": (_i, [_vp, _i, _i, _i]),
 }
 
 
@@ -234,6 +236,16 @@ class Engine:
     # -- population-level operations --------------------------------------------
     def seed(self, seed: int):
         call("spe_seed", self.h, C.c_uint32(int(seed) & 0xFFFFFFFF))
+
+    def initialize_pop(self, first, count, support_size, itemsize, nitems=(8, 8), exponent=(0.0, 0.0),
+                       scaling=(0.0, 0.0), phaserange=0.0, suppcut=0.0):
+        self.reserve(first + count)
+        call("spe_initialize_pop", self.h, int(first), int(count), int(support_size), float(itemsize[0]),
+             float(itemsize[1]), int(nitems[0]), int(nitems[1]), float(exponent[0]), float(exponent[1]),
+             float(scaling[0]), float(scaling[1]), float(phaserange), float(suppcut))
+
+    def copy(self, src, dst, count):
+        call("spe_copy", self.h, int(src), int(dst), int(count))
 
     def reshift(self, first, count, ref_slot=-1, ref_density=None, minr=0.0, maxr=2.0):
         r = None if ref_density is None else np.ascontiguousarray(ref_density, dtype=np.complex64)

@@ -132,6 +132,32 @@ int draw_children(std::mt19937& g, int P, const int* order, float suppdim, int n
   return 0;
 }
 
+// Solver::Initialize_rec's draws (src/solver.cpp:882-906), individual by
+// individual, in the reference's order and float arithmetic.
+void draw_init(std::mt19937& g, int count, int support_size, const float itemsize[2], const int nitems_in[2],
+               const float exponent_in[2], const float scaling_in[2], float phase_in, std::vector<InitDraw>& inds,
+               std::vector<InitItem>& items) {
+  std::uniform_real_distribution<float> dist(0, 1);
+  auto rnd = [&](float lo, float hi) { return dist(g) * (hi - lo) + lo; };
+  inds.assign(count, InitDraw{});
+  items.clear();
+  for (int k = 0; k < count; ++k) {
+    InitDraw& d = inds[k];
+    d.nitems = int(rnd(nitems_in[0], nitems_in[1] + 0.99));
+    d.exponent = rnd(exponent_in[0], exponent_in[1]);
+    d.scaling = rnd(scaling_in[0], scaling_in[1]);
+    d.first_item = (int)items.size();
+    for (int i = 0; i < d.nitems; ++i) {
+      InitItem it;
+      it.sigma = (float)(std::sqrt(rnd(std::pow(itemsize[0], 2), std::pow(itemsize[1], 2))) / 2.);
+      it.cx = rnd(it.sigma, support_size - it.sigma);
+      it.cy = rnd(it.sigma, support_size - it.sigma);
+      it.phase = rnd(-phase_in * M_PI, phase_in * M_PI);
+      items.push_back(it);
+    }
+  }
+}
+
 }  // namespace spe
 
 extern "C" int spe_crossover_draws(uint32_t seed, int count, const int32_t* order, float suppdim, int n,

@@ -27,6 +27,20 @@ struct ChildDraw {
 int draw_children(std::mt19937& g, int count, const int* order, float suppdim, int n, float crossbalance,
                   float crossexp, float crossftin, std::vector<ChildDraw>& out, std::vector<int>& cmaps);
 
+// Random draws of one starting individual (Solver::Initialize_rec,
+// src/solver.cpp:880-906): disc items of radius sigma at (cx, cy) inside the
+// support box, with a phase each; the modulus exponent and the scaling.
+struct InitItem {
+  float sigma, cx, cy, phase;
+};
+struct InitDraw {
+  int first_item, nitems;
+  float exponent, scaling;
+};
+void draw_init(std::mt19937& g, int count, int support_size, const float itemsize[2], const int nitems[2],
+               const float exponent[2], const float scaling[2], float phase, std::vector<InitDraw>& inds,
+               std::vector<InitItem>& items);
+
 // Everything a size-specialised sequence needs about one call.
 struct Ctx {
   int n;
@@ -87,6 +101,8 @@ struct SizeOps {
   int (*col_widths)(int* out);
   int (*row_widths)(int* out);
   int default_cols, default_rows;
+  // partials of the column pass: sum over A >= 0 of |FFT+(rho)|^2 and A^2
+  cudaError_t (*known_power)(const Ctx&, double* partials);
 };
 
 const SizeOps* size_ops(int n);

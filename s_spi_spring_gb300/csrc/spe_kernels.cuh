@@ -581,6 +581,33 @@ struct OpRowsPeak : OpBase {
   }
 };
 
+// column pass on the row-transformed starting density: FFT+ (y) gives F;
+// sum over known pixels of |F|^2 and of A^2 (Initialize_rec's scaling,
+// src/solver.cpp:938-947); nothing is stored
+struct OpColsKnownPower : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = 0, NSUM = 2, NMAX = 0;
+  const float2* T;
+  const float* A;
+  int n;
+  struct Acc {
+    float f2 = 0.f, a2 = 0.f;
+    __device__ void values(double (&v)[NRED]) const {
+      v[0] = f2;
+      v[1] = a2;
+      v[2] = v[3] = 0.0;
+    }
+  };
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t, int, int y, int x, Acc& acc) const {
+    const float a = __ldg(A + (size_t)y * n + x);
+    if (a >= 0.f) {
+      acc.f2 += v.x * v.x + v.y * v.y;
+      acc.a2 += a * a;
+    }
+  }
+};
+
 // ---- generic 2D transforms on arrays of items (item p at offset p*N*N)
 
 // column pass: src -> FFT(S) (y) -> dst

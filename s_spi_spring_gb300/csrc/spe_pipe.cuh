@@ -47,8 +47,10 @@ struct ColCfg {  // column pass with W columns per tile
   static constexpr int C_A = align128(N * W * 4);
   static constexpr int STAGE = C_T + C_A;
   static constexpr size_t SMEM = (size_t)TWB + 2 * STAGE;
-  // two CTAs per SM when the registers of E elements per thread allow it
-  static constexpr int MINB = (E <= 8 && NT <= 512) ? 2 : 1;
+  // resident CTAs per SM the register budget (64 per thread for E <= 8,
+  // 128 above) must allow
+  static constexpr int MINB_RAW = 65536 / (NT * (E <= 8 ? 64 : 128));
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
 };
 
 template <int N, int W>
@@ -65,7 +67,8 @@ struct RowCfg {  // row pass with W rows per tile
   static constexpr int STAGE = R_T + R_R + R_S;
   static constexpr int R_X = align128(LayPad<N, W>::SIZE * 8);
   static constexpr size_t SMEM = (size_t)TWB + R_X + 2 * STAGE;
-  static constexpr int MINB = (NT <= 256 || (E <= 8 && NT <= 512)) ? 2 : 1;
+  static constexpr int MINB_RAW = 65536 / (NT * (E <= 8 ? 96 : 128));
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
 };
 
 template <int N>

@@ -21,6 +21,8 @@ using namespace spe_detail;
 namespace spe {
 
 __global__ void k_reduce_peak(const double* __restrict__ part, int count, int tpi, double* out, int ostride, int oslot);
+__global__ void k_reduce(const double* __restrict__ part, int count, int tpi, int k, int is_max, double* out,
+                         int ostride, int oslot);
 
 // complex sum of item idx[p] (or p) per block, double accumulation
 __global__ void k_complex_sum(const float2* __restrict__ src, size_t npix, const int* __restrict__ idx,
@@ -262,6 +264,56 @@ __global__ void k_cross_finish(const float2* __restrict__ C, const int* __restri
   S[d] = update_support ? s : S[(size_t)self_slot[k] * npix + i];
 }
 
+// ---- starting population (Solver::Initialize_rec, src/solver.cpp:880-957):
+// a disc support of diameter ss centred in the field; inside it the density
+// is a sum of disc profiles 2 sigma sin(acos(r/sigma)) with a phase each,
+// its modulus raised to `exponent`
+__global__ void k_init_objects(float2* __restrict__ rho, int* __restrict__ S, const InitDraw* __restrict__ inds,
+                               const InitItem* __restrict__ items, int first, int n, int ss) {
+  const InitDraw d = inds[blockIdx.y];
+  const size_t npix = (size_t)n * n;
+  const size_t base = (size_t)(first + blockIdx.y) * npix;
+  const int off = n / 2 - ss / 2;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % n) - off, iy = (int)(i / n) - off;
+    float2 v = make_float2(0.f, 0.f);
+    int s = 0;
+    if (ix >= 0 && iy >= 0 && ix < ss && iy < ss) {
+      const double dx = ix - ss / 2., dy = iy - ss / 2.;
+      if (sqrt(dx * dx + dy * dy) <= ss / 2.) {
+        s = 1;
+        for (int k = 0; k < d.nitems; ++k) {
+          const InitItem it = items[d.first_item + k];
+          const float ax = ix - it.cx, ay = iy - it.cy;
+          const float rad = sqrtf(ax * ax + ay * ay);
+          if (rad < it.sigma) {
+            const float val = (float)(2. * (double)it.sigma * (double)sinf(acosf(rad / it.sigma)));
+            float sn, cs;
+            sincosf(it.phase, &sn, &cs);
+            v.x += val * cs;
+            v.y += val * sn;
+          }
+        }
+        const float mod = hypotf(v.x, v.y);
+        if (mod > 0.f) {
+          const float pw = powf(mod, d.exponent);
+          v = make_float2(v.x / mod * pw, v.y / mod * pw);
+        }
+      }
+    }
+    rho[base + i] = v;
+    S[base + i] = s;
+  }
+}
+
+// density of individual first+k *= scale[k]
+__global__ void k_scale_items(float2* __restrict__ rho, const float* __restrict__ scale, int first, size_t npix) {
+  const float f = scale[blockIdx.y];
+  float2* r = rho + (size_t)(first + blockIdx.y) * npix;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x)
+    r[i] = make_float2(r[i].x * f, r[i].y * f);
+}
+
 }  // namespace spe
 
 namespace {
@@ -478,6 +530,76 @@ int spe_average_module(spe_engine* e, int first, int count, const float* errors,
     return rc;
   if (out) CK(cudaMemcpyAsync(out, e->avg_mod, npix * sizeof(float), cudaMemcpyDeviceToHost, e->st), "download");
   CK(cudaStreamSynchronize(e->st), "synchronize");
+  return SPE_OK;
+}
+
+int spe_initialize_pop(spe_engine* e, int first, int count, int support_size, float itemsize_min, float itemsize_max,
+                       int nitems_min, int nitems_max, float exponent_min, float exponent_max, float scaling_min,
+                       float scaling_max, float phaserange, float suppcut) {
+  (void)suppcut;  // accepted and unused by the reference as well (src/solver.cpp:880-957)
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if ((rc = need_amp(e))) return rc;
+  if (support_size < 1 || support_size > e->n) return fail(SPE_ERR_INVALID, "support size %d outside [1, %d]",
+                                                            support_size, e->n);
+  if (count == 0) return SPE_OK;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  const float isz[2] = {itemsize_min, itemsize_max}, ex[2] = {exponent_min, exponent_max},
+              sc[2] = {scaling_min, scaling_max};
+  const int ni[2] = {nitems_min, nitems_max};
+  std::vector<spe::InitDraw> inds;
+  std::vector<spe::InitItem> items;
+  spe::draw_init(e->rng, count, support_size, isz, ni, ex, sc, phaserange, inds, items);
+  const int tc = e->ops->tiles_cols;
+  const size_t need = (size_t)count * tc * spe::NRED * sizeof(double) + inds.size() * sizeof(spe::InitDraw) +
+                      (items.size() + 1) * sizeof(spe::InitItem) + count * (sizeof(float) + 2 * sizeof(double)) +
+                      4096;
+  if ((rc = ensure_work(e, need))) return rc;
+  Carve cv{(char*)e->work};
+  double* part = cv.take<double>((size_t)count * tc * spe::NRED);
+  spe::InitDraw* dinds = cv.take<spe::InitDraw>(count);
+  spe::InitItem* ditems = cv.take<spe::InitItem>(items.size() + 1);
+  float* dscale = cv.take<float>(count);
+  double* sums = cv.take<double>((size_t)count * 2);
+  CK(cudaMemcpyAsync(dinds, inds.data(), count * sizeof(spe::InitDraw), cudaMemcpyHostToDevice, e->st), "draws");
+  if (!items.empty())
+    CK(cudaMemcpyAsync(ditems, items.data(), items.size() * sizeof(spe::InitItem), cudaMemcpyHostToDevice, e->st),
+       "items");
+  const dim3 grid((unsigned)std::min<size_t>((e->npix + 255) / 256, 1024), (unsigned)count);
+  spe::k_init_objects<<<grid, 256, 0, e->st>>>(e->rho, e->S, dinds, ditems, first, e->n, support_size);
+  CK(cudaGetLastError(), "object synthesis");
+  CK(e->ops->known_power(make_ctx(e, first, count), part), "power transform");
+  spe::k_reduce<<<(count + 127) / 128, 128, 0, e->st>>>(part, count, tc, 0, 0, sums, 2, 0);
+  spe::k_reduce<<<(count + 127) / 128, 128, 0, e->st>>>(part, count, tc, 1, 0, sums, 2, 1);
+  CK(cudaGetLastError(), "power reduce");
+  std::vector<double> hs((size_t)count * 2);
+  CK(cudaMemcpyAsync(hs.data(), sums, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, e->st), "sums");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  std::vector<float> scale(count);
+  for (int k = 0; k < count; ++k) {
+    const float norm = (float)hs[2 * k], norm_new = (float)hs[2 * k + 1];
+    scale[k] = std::sqrt(norm_new / norm) * inds[k].scaling;
+  }
+  CK(cudaMemcpyAsync(dscale, scale.data(), count * sizeof(float), cudaMemcpyHostToDevice, e->st), "scales");
+  spe::k_scale_items<<<grid, 256, 0, e->st>>>(e->rho, dscale, first, e->npix);
+  CK(cudaGetLastError(), "scaling");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  return SPE_OK;
+}
+
+int spe_copy(spe_engine* e, int src, int dst, int count) {
+  int rc = check_range(e, src, count);
+  if (rc) return rc;
+  if ((rc = check_range(e, dst, count))) return rc;
+  if (count == 0 || src == dst) return SPE_OK;
+  if (dst < src + count && src < dst + count) return fail(SPE_ERR_INVALID, "overlapping source and destination slots");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  CK(cudaMemcpyAsync(e->rho + (size_t)dst * e->npix, e->rho + (size_t)src * e->npix,
+                     (size_t)count * e->npix * sizeof(float2), cudaMemcpyDeviceToDevice, e->st),
+     "copy density");
+  CK(cudaMemcpyAsync(e->S + (size_t)dst * e->npix, e->S + (size_t)src * e->npix,
+                     (size_t)count * e->npix * sizeof(int), cudaMemcpyDeviceToDevice, e->st),
+     "copy support");
   return SPE_OK;
 }
 

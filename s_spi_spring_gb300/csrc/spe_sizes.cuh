@@ -33,8 +33,6 @@ cudaError_t launch_pass(const Op& op, int count, cudaStream_t st, const float2* 
   return cudaGetLastError();
 }
 
-// persistent grid: two CTAs per SM (shared memory allows two at the sizes
-// that matter), never more CTAs than tiles
 inline int sm_count() {
   static int count[64] = {0};
   int dev = 0;
@@ -83,15 +81,33 @@ struct DefaultTiles {
   static constexpr int rows = (N <= 256) ? 8 : (N == 384 ? 8 : (N <= 512 ? 4 : (N <= 1024 ? 2 : 1)));
 };
 
+// persistent grid size: the CTAs that fit on all SMs at once (occupancy
+// queried once per kernel and device), never more than the tiles
+template <class K>
+int resident_ctas(K kern, int threads, size_t smem, int* cache) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 64) dev = 63;
+  if (cache[dev] == 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    cache[dev] = per_sm * sm_count();
+  }
+  return cache[dev];
+}
+
 template <int N, int W>
 cudaError_t launch_cols_project(const Ctx& c) {
   using P = ColCfg<N, W>;
   auto kern = k_cols_project<N, W>;
   static unsigned long long configured = 0ull;
+  static int resident[64] = {0};
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
-  const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
+  const int slots = resident_ctas(kern, P::NT, P::SMEM, resident);
+  const int grid = tiles < slots ? tiles : slots;
   kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
   return cudaGetLastError();
 }
@@ -101,10 +117,12 @@ cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
   using P = RowCfg<N, W>;
   auto kern = k_rows_iterate<N, W, UPD>;
   static unsigned long long configured = 0ull;
+  static int resident[64] = {0};
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
-  const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
+  const int slots = resident_ctas(kern, P::NT, P::SMEM, resident);
+  const int grid = tiles < slots ? tiles : slots;
   kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.rho, c.S, c.first, c.count, scale, beta, g, c.tw);
   return cudaGetLastError();
 }
@@ -397,6 +415,18 @@ struct SizeImpl {
     return corr_peak_idx_t<+1>(c, D, Dref, xi, ri, minr, maxr, norm_d, norm_ref, scratch, partials);
   }
 
+  // partials (rows of the column pass): sum_{A>=0} |FFT+(rho)|^2, sum_{A>=0} A^2
+  static cudaError_t known_power(const Ctx& c, double* partials) {
+    SPE_TRY((launch_pass<N, AX_ROWS>(rows_forward<SRC_RHO>(c, c.rho, c.T, Gate{}, nullptr), c.count, c.st, c.tw)));
+    OpColsKnownPower kp;
+    kp.first = c.first;
+    kp.partials = partials;
+    kp.T = c.T;
+    kp.A = c.A;
+    kp.n = N;
+    return launch_pass<N, AX_COLS>(kp, c.count, c.st, c.tw);
+  }
+
   static const SizeOps* table() {
     static const SizeOps t = {N,
                               N / TileW<N>::rows,
@@ -415,7 +445,8 @@ struct SizeImpl {
                               &SizeImpl<N>::col_widths,
                               &SizeImpl<N>::row_widths,
                               DefaultTiles<N>::cols,
-                              DefaultTiles<N>::rows};
+                              DefaultTiles<N>::rows,
+                              &SizeImpl<N>::known_power};
     return &t;
   }
 };

@@ -240,6 +240,15 @@ class Solver:
             r._set_metrics(m)
         return None
 
+    # -- starting populations (src/solver.cpp:824-957, wrapper.cpp:278-298) ------
+    def InitializePop(self, popsize, suppsize, itemsize, nitems=8, exponent=0, scaling=0, phaserange=0, suppcut=0):
+        """``Solver::Initialize_pop``: `popsize` random starting individuals."""
+        pair = lambda v: (v[0], v[1]) if np.ndim(v) else (v, v)
+        self.engine.initialize_pop(0, int(popsize), int(suppsize), pair(itemsize), pair(nitems), pair(exponent),
+                                   pair(scaling), float(phaserange), float(suppcut))
+        d, s = self.engine.download(0, int(popsize))
+        return [Reconstruction(d[i], s[i]) for i in range(int(popsize))]
+
     # -- population-level operations (src/solver.cpp:511-817) --------------------
     def Reshift(self, reconstruction, reference):
         """Aligns each reconstruction to `reference` (translation, global phase,

@@ -21,6 +21,10 @@ from oracle import ref_solver  # noqa: E402
 from s_spi_spring_gb300 import synthetic  # noqa: E402
 
 PREP_CASES = [(64, 5, (-1, -1)), (128, 6, (-1, -1)), (128, 6, (60, 70)), (96, 8, (50, 40))]
+# (n, seed, count, support_size, itemsize, nitems, exponent, scaling, phase)
+INIT_CASES = [(64, 42, 3, 30, (6.0, 27.0), (2, 8), (0.5, 0.5), (0.5, 1.5), 0.2),
+              (128, 7, 4, 50, (5.0, 30.0), (1, 12), (0.3, 1.0), (1.0, 1.0), 0.5),
+              (128, 11, 2, 64, (10.0, 10.0), (8, 8), (0.0, 0.0), (0.8, 1.2), 0.0)]
 DRAW_CASES = [(17, 16, 1.0, 1.0), (42, 33, 0.5, 2.0), (7, 8, 0.0, 0.7), (123, 64, 1.0, 1.0)]
 
 
@@ -55,6 +59,13 @@ def main():
         out[f"draw{k}_draws"] = d
         out[f"draw{k}_rot"] = r
         out[f"draw{k}_cmaps"] = cm
+    for k, (n, seed, count, ss, isz, nit, ex, sc, ph) in enumerate(INIT_CASES):
+        I = pattern(n, seed)
+        d, su = ref_solver.initialize_pop(I, count, ss, isz, nit, ex, sc, ph, seed)
+        out[f"init{k}_in"] = I
+        out[f"init{k}_params"] = np.array([n, seed, count, ss, *isz, *nit, *ex, *sc, ph], np.float64)
+        out[f"init{k}_density"] = d
+        out[f"init{k}_support"] = su.astype(np.int8)
     np.savez_compressed(os.path.join(HERE, "ref_host.npz"), **out)
 
 

@@ -146,3 +146,53 @@ def test_solver_population_methods():
     kids = sol.Crossover(recs, recs[0], avg, 0.6, 0.4)
     assert len(kids) == P and all(k.get_error() == r.get_error() for k, r in zip(kids, recs))
     sol.Sequence(kids) if sol._ops else None
+
+
+_GOLD = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "ref_host.npz"))
+
+
+@pytest.mark.parametrize("case", sorted({k.split("_")[0] for k in _GOLD.files if k.startswith("init")}))
+def test_initialize_pop_vs_reference_fixture(case):
+    """spe_initialize_pop against the reference's own Solver::Initialize_pop
+    (run on the CPU with a double-precision DFT as its transform): supports
+    exact, densities within 1e-4 relative (float disc profiles and the
+    FP32 FFT of the scaling step)."""
+    from s_spi_spring_gb300.spring_core.phase_retrieval import Solver
+    p = _GOLD[f"{case}_params"]
+    n, seed, count, ss = (int(v) for v in p[:4])
+    sol = Solver(_GOLD[f"{case}_in"], use_bounds=False, gpus=[0], seed=seed)
+    recs = sol.InitializePop(count, ss, itemsize=[p[4], p[5]], nitems=[int(p[6]), int(p[7])],
+                             exponent=[p[8], p[9]], scaling=[p[10], p[11]], phaserange=p[12])
+    ref_d, ref_s = _GOLD[f"{case}_density"], _GOLD[f"{case}_support"].astype(np.int32)
+    for k in range(count):
+        d, s = recs[k].get_density(), recs[k].get_support()
+        assert np.array_equal(s, ref_s[k])
+        assert np.array_equal(d != 0, ref_d[k] != 0)
+        assert np.linalg.norm(d - ref_d[k]) <= 1e-4 * np.linalg.norm(ref_d[k])
+
+
+def test_initialize_pop_then_copy_slots():
+    """Population slots: initialise [2, 6), copy them to [8, 12) and check the
+    copy is bit-exact and the source untouched; a second initialisation
+    continues the generator (new individuals differ)."""
+    n = 128
+    I, _, _ = synthetic.polygon_pattern(seed=3, n=n, diameter=40)
+    eng = _lib.Engine(n, 0)
+    eng.set_amplitudes(_lib.prepare_pattern(I, (-1, -1), True))
+    eng.seed(9)
+    eng.initialize_pop(2, 4, 50, (5.0, 25.0), (2, 9), (0.5, 0.5), (0.5, 1.5), 0.3)
+    d0, s0 = eng.download(2, 4)
+    eng.copy(2, 8, 4)
+    d1, s1 = eng.download(8, 4)
+    assert np.array_equal(d0.view(np.uint32), d1.view(np.uint32)) and np.array_equal(s0, s1)
+    assert np.array_equal(eng.download(2, 4)[0].view(np.uint32), d0.view(np.uint32))
+    eng.initialize_pop(2, 4, 50, (5.0, 25.0), (2, 9), (0.5, 0.5), (0.5, 1.5), 0.3)
+    assert not np.array_equal(eng.download(2, 4)[0], d0)
+    # the oracle, from the same generator state, draws the same first population
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    od, osu = o.initialize_pop(A, o.ContextRNG(9), 4, 50, (5.0, 25.0), (2, 9), (0.5, 0.5), (0.5, 1.5), 0.3)
+    assert np.array_equal(osu, s0)
+    for k in range(4):
+        assert np.linalg.norm(d0[k] - od[k]) <= 1e-4 * np.linalg.norm(od[k])
+    with pytest.raises(_lib.EngineError):
+        eng.copy(8, 10, 4)  # overlapping ranges are rejected

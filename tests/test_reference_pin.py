@@ -63,3 +63,20 @@ def test_live_reference_build_matches_engine():
     d, r, cm = ref_solver.crossover_draws(96, errors, best, 5, 0.3, 1.5, 0.7)
     g, gr, gc = _lib.crossover_draws(5, o.sorted_indexes(errors), o.suppdim_of(best, 96), 96, 0.3, 1.5, 0.7)
     assert np.array_equal(d[:, :10], g[:, :10]) and np.array_equal(r, gr) and np.array_equal(cm, gc)
+
+
+@pytest.mark.parametrize("case", _cases("init"))
+def test_initialize_pop_oracle_vs_reference(case):
+    """The oracle's restatement of Solver::Initialize_pop against the
+    reference's own run (same draws, disc profiles, exponent and scaling)."""
+    p = GOLD[f"{case}_params"]
+    n, seed, count, ss = (int(v) for v in p[:4])
+    isz, nit, ex, sc, ph = (p[4], p[5]), (int(p[6]), int(p[7])), (p[8], p[9]), (p[10], p[11]), p[12]
+    I = GOLD[f"{case}_in"]
+    A = o.prepare_pattern(I, (-1, -1), False)
+    d, s = o.initialize_pop(A, o.ContextRNG(seed), count, ss, isz, nit, ex, sc, ph)
+    ref_d, ref_s = GOLD[f"{case}_density"], GOLD[f"{case}_support"]
+    assert np.array_equal(s, ref_s.astype(np.int32))
+    for k in range(count):
+        assert np.array_equal(d[k] != 0, ref_d[k] != 0)
+        assert np.linalg.norm(d[k] - ref_d[k]) <= 1e-5 * np.linalg.norm(ref_d[k])
