@@ -51,7 +51,9 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
-    ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
+    ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
+    ap.add_argument("--schedule", default="", help="chunk,lanes iteration schedule (implies --no-tune)")
     return ap.parse_args()
 
 
@@ -195,7 +197,7 @@ def run_engine(args):
     stream = torch.cuda.Stream(device=local)
     eng.set_stream(stream.cuda_stream)
     eng.upload(0, dens, S)
-    tiles = eng.tiles() if args.no_tune else eng.autotune(0, POP, 10)
+    tiles, sched = configure(eng, args, tune_iters=10)
     eng.synchronize()
 
     def barrier():
@@ -291,7 +293,8 @@ def run_engine(args):
                                f"{args.iters} iterations per step",
                    "pattern": N, "population": POP, "iterations_per_step": args.iters,
                    "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (320 MiB working set)",
-                   "tiles": {"cols": tiles[0], "rows": tiles[1], "autotuned": not args.no_tune}},
+                   "tiles": {"cols": tiles[0], "rows": tiles[1]},
+                   "schedule": {"chunk": sched[0], "lanes": sched[1]}, "autotuned": fixed_config(args) is None},
         "e2e": {"value": round(e2e_value, 1), "unit": "iter*individuals/s",
                 "h2d_bytes_per_step": int(h_dens.numel() * 4 + h_supp.numel() * 4),
                 "d2h_bytes_per_step": int(h_out.numel() * 4)},
@@ -360,6 +363,27 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def fixed_config(args):
+    """(tiles, schedule) given on the command line, or None to autotune."""
+    if not (args.no_tune or args.tiles or args.schedule):
+        return None
+    t = tuple(int(v) for v in args.tiles.split(",")) if args.tiles else (0, 0)
+    s = tuple(int(v) for v in args.schedule.split(",")) if args.schedule else (0, 1)
+    return t, s
+
+
+def configure(eng, args, tune_iters=10):
+    """Tile widths and iteration schedule: fixed, or autotuned on the
+    resident population (densities restored)."""
+    fixed = fixed_config(args)
+    if fixed is None:
+        eng.autotune(0, POP, tune_iters)
+    else:
+        eng.set_tiles(*fixed[0])
+        eng.set_schedule(*fixed[1])
+    return eng.tiles(), eng.schedule()
+
+
 def run_profile_case(args):
     """One RAAR call on the resident workload (for ncu captures)."""
     from s_spi_spring_gb300 import _lib
@@ -367,12 +391,14 @@ def run_profile_case(args):
     eng = _lib.Engine(N, 0)
     eng.set_amplitudes(A)
     eng.upload(0, dens, S)
-    if not args.no_tune:
-        eng.autotune(0, POP, 4)
+    # the tuned configuration is fixed on the command line, so that the
+    # profiled launches are the configuration's own (no tuning trials)
+    args.no_tune = True
+    tiles, sched = configure(eng, args)
     eng.raar(0, POP, 1, BETA, 0.0)  # warm-up
     eng.raar(0, POP, args.profile_iters, BETA, 0.0)
     eng.synchronize()
-    print(json.dumps({"profile_case": "RAAR", "iterations": args.profile_iters, "tiles": eng.tiles()}))
+    print(json.dumps({"profile_case": "RAAR", "iterations": args.profile_iters, "tiles": tiles, "schedule": sched}))
 
 
 def main():

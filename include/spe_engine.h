@@ -204,6 +204,14 @@ int spe_initialize_pop(spe_engine* e, int first, int count, int support_size, fl
  * Overlapping source and destination ranges are rejected. */
 int spe_copy(spe_engine* e, int src, int dst, int count);
 
+/* Gathers individuals into a contiguous range: slot dst_first+k receives
+ * slot src[k] (density and support), k < count, in one launch.  No source
+ * slot may lie inside the destination range; a slot may be listed twice.
+ * (No reference counterpart: the reference keeps each individual in host
+ * memory; this lets the Python front end's reordered lists stay on the
+ * device.) */
+int spe_gather(spe_engine* e, const int32_t* src, int count, int dst_first);
+
 /* Host-only: the random draws of Solver::Crossover (src/solver.cpp:750-801)
  * for `count` children from std::mt19937(seed), given the error order and
  * suppdim.  draws: count*11 ints (p1, p2, p3, crossft, squaresizex,
@@ -220,11 +228,23 @@ int spe_crossover_draws(uint32_t seed, int count, const int32_t* order, float su
 int spe_set_tiles(spe_engine* e, int cols, int rows);
 int spe_get_tiles(spe_engine* e, int* cols, int* rows);
 
+/* Iteration schedule (no reference counterpart; the reference runs one
+ * individual per context): HIO / RAAR / ER calls process the range in blocks
+ * of `chunk` individuals (0: the whole range at once), each block through
+ * all its iterations before the next, so that a block's density, scratch
+ * and support stay in L2 between iterations.  lanes = 2 runs two blocks at a
+ * time on two streams (forked from and joined into the engine's stream),
+ * each kernel on half the SMs.  Results do not depend on the schedule. */
+int spe_set_schedule(spe_engine* e, int chunk, int lanes);
+int spe_get_schedule(spe_engine* e, int* chunk, int* lanes);
+
 /* Autotuner (no reference counterpart; the reference has fixed 32x32
  * blocks, gpu_context.h:17-21): times every compiled tile width of the
  * iteration kernels on the resident population [first, first+count) with
- * `iterations` RAAR steps per trial, keeps the fastest and restores the
- * densities.  cols / rows (may be NULL) receive the choice. */
+ * `iterations` RAAR steps per trial, then the schedule (spe_set_schedule,
+ * blocks that fit in L2), keeps the fastest and restores the densities.
+ * cols / rows (may be NULL) receive the widths; spe_get_schedule the
+ * schedule. */
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows);
 
 /* Allocation-free HIO / RAAR / ER (no counterpart in the reference).

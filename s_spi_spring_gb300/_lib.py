@@ -69,10 +69,13 @@ SIGNATURES = {
     "spe_crossover_draws": (_i, [C.c_uint32, _i, _ip, _f, _i, _f, _f, _f, _ip, _fp, _ip, _i, _ip]),
     "spe_set_tiles": (_i, [_vp, _i, _i]),
     "spe_get_tiles": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
+    "spe_set_schedule": (_i, [_vp, _i, _i]),
+    "spe_get_schedule": (_i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
     "spe_autotune": (_i, [_vp, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)]),
     "spe_iterate_noalloc": (_i, [_i, _vp, _vp, _vp, _i, _i, _i, _f, _f, _vp]),
     "spe_initialize_pop": (_i, [_vp, _i, _i, _i, _f, _f, _i, _i, _f, _f, _f, _f, _f, _f]),
     "spe_copy": (_i, [_vp, _i, _i, _i]),
+    "spe_gather": (_i, [_vp, _ip, _i, _i]),
 }
 
 
@@ -228,6 +231,14 @@ class Engine:
         call("spe_get_tiles", self.h, C.byref(a), C.byref(b))
         return a.value, b.value
 
+    def set_schedule(self, chunk=0, lanes=1):
+        call("spe_set_schedule", self.h, int(chunk), int(lanes))
+
+    def schedule(self):
+        a, b = C.c_int(), C.c_int()
+        call("spe_get_schedule", self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def autotune(self, first, count, iterations=10):
         a, b = C.c_int(), C.c_int()
         call("spe_autotune", self.h, int(first), int(count), int(iterations), C.byref(a), C.byref(b))
@@ -246,6 +257,10 @@ class Engine:
 
     def copy(self, src, dst, count):
         call("spe_copy", self.h, int(src), int(dst), int(count))
+
+    def gather(self, src_slots, dst_first):
+        src = np.ascontiguousarray(src_slots, dtype=np.int32)
+        call("spe_gather", self.h, iptr(src), int(src.size), int(dst_first))
 
     def reshift(self, first, count, ref_slot=-1, ref_density=None, minr=0.0, maxr=2.0):
         r = None if ref_density is None else np.ascontiguousarray(ref_density, dtype=np.complex64)

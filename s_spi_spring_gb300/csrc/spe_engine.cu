@@ -220,7 +220,57 @@ spe::Ctx make_ctx(spe_engine* e, int first, int count) {
   c.tw = e->tw;
   c.partials = e->partials;
   c.red = e->red;
+  c.grid_div = 1;
+  c.mark = nullptr;
   return c;
+}
+
+size_t l2_bytes(int dev) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) != cudaSuccess || v <= 0) v = 64 << 20;
+  return (size_t)v;
+}
+
+// Runs `iters` iterations on [first, first+count) in blocks of `chunk`
+// individuals, each block through all its iterations before the next (the
+// individuals are independent, so the result equals one call on the whole
+// range).  lanes = 2 runs consecutive blocks on the engine's stream and a
+// second stream, forked from and joined back into the engine's stream, with
+// every persistent kernel on half the resident CTAs.
+int run_iterations(spe_engine* e, int first, int count, int upd, int iters, float beta, const spe::Gate& g, int chunk,
+                   int lanes, int wc, int wr) {
+  if (chunk <= 0 || chunk > count) chunk = count;
+  const int nblocks = (count + chunk - 1) / chunk;
+  if (lanes < 2 || nblocks < 2) {
+    for (int b = 0; b < nblocks; ++b) {
+      const int f = first + b * chunk, k = std::min(chunk, first + count - f);
+      CK(e->ops->iterate(make_ctx(e, f, k), upd, iters, beta, g, wc, wr), "iteration kernels");
+    }
+    return SPE_OK;
+  }
+  if (!e->lane2) {
+    CK(cudaStreamCreateWithFlags(&e->lane2, cudaStreamNonBlocking), "lane stream");
+    CK(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming), "lane event");
+    CK(cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming), "lane event");
+    CK(cudaEventCreateWithFlags(&e->phase, cudaEventDisableTiming), "lane event");
+  }
+  CK(cudaEventRecord(e->fork, e->st), "fork");
+  CK(cudaStreamWaitEvent(e->lane2, e->fork, 0), "fork");
+  for (int b = 0; b < nblocks; ++b) {
+    const int f = first + b * chunk, k = std::min(chunk, first + count - f);
+    spe::Ctx c = make_ctx(e, f, k);
+    c.st = (b & 1) ? e->lane2 : e->st;
+    c.grid_div = 2;
+    // the second lane starts once the first has passed its first column
+    // pass, so that one lane's row passes (HBM-bound) run beside the other
+    // lane's column passes (arithmetic-bound)
+    if (b == 0) c.mark = e->phase;
+    if (b == 1) CK(cudaStreamWaitEvent(e->lane2, e->phase, 0), "phase");
+    CK(e->ops->iterate(c, upd, iters, beta, g, wc, wr), "iteration kernels");
+  }
+  CK(cudaEventRecord(e->join, e->lane2), "join");
+  CK(cudaStreamWaitEvent(e->st, e->join, 0), "join");
+  return SPE_OK;
 }
 
 size_t max_tiles(const spe::SizeOps* o) { return (size_t)std::max(o->tiles_rows, o->tiles_cols); }
@@ -275,9 +325,7 @@ int do_iterate(spe_engine* e, int first, int count, int upd, int iters, float be
   if (count == 0) return SPE_OK;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   const spe::Gate g = (upd == 1) ? gate_raar(real) : gate_er(real);
-  CK(e->ops->iterate(make_ctx(e, first, count), upd, iters, beta, g, e->tile_cols, e->tile_rows),
-     "iteration kernels");
-  return SPE_OK;
+  return run_iterations(e, first, count, upd, iters, beta, g, e->chunk, e->lanes, e->tile_cols, e->tile_rows);
 }
 
 int do_shrinkwrap(spe_engine* e, int first, int count, float sigma, bool absolute, float threshold, int pixels) {
@@ -381,6 +429,13 @@ int spe_destroy(spe_engine* e) {
   cudaFree(e->avg_mod);
   cudaFree(e->ref);
   cudaFree(e->work);
+  if (e->lane2) {
+    cudaStreamSynchronize(e->lane2);
+    cudaStreamDestroy(e->lane2);
+    cudaEventDestroy(e->fork);
+    cudaEventDestroy(e->join);
+    cudaEventDestroy(e->phase);
+  }
   cudaStreamDestroy(e->own);
   delete e;
   return SPE_OK;
@@ -614,6 +669,21 @@ int spe_set_tiles(spe_engine* e, int cols, int rows) {
   return SPE_OK;
 }
 
+int spe_set_schedule(spe_engine* e, int chunk, int lanes) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  if (chunk < 0 || lanes < 1 || lanes > 2) return fail(SPE_ERR_INVALID, "chunk must be >= 0 and lanes 1 or 2");
+  e->chunk = chunk;
+  e->lanes = lanes;
+  return SPE_OK;
+}
+
+int spe_get_schedule(spe_engine* e, int* chunk, int* lanes) {
+  if (!e || !chunk || !lanes) return fail(SPE_ERR_INVALID, "null argument");
+  *chunk = e->chunk;
+  *lanes = e->lanes;
+  return SPE_OK;
+}
+
 int spe_get_tiles(spe_engine* e, int* cols, int* rows) {
   if (!e || !cols || !rows) return fail(SPE_ERR_INVALID, "null argument");
   *cols = e->tile_cols > 0 ? e->tile_cols : e->ops->default_cols;
@@ -624,7 +694,9 @@ int spe_get_tiles(spe_engine* e, int* cols, int* rows) {
 // Times the compiled tile widths of the iteration kernels on the resident
 // population [first, first+count) (RAAR, `iterations` per trial, median of
 // three) -- first the column pass with the current row width, then the row
-// pass -- keeps the fastest and restores the densities.
+// pass -- then the schedule (block size and lanes, blocks that fit in L2;
+// kept only when 2% faster than the whole range), keeps the fastest and
+// restores the densities.
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows) {
   int rc = check_range(e, first, count);
   if (rc) return rc;
@@ -638,13 +710,13 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
   CK(cudaEventCreate(&a), "event");
   CK(cudaEventCreate(&b), "event");
   const spe::Gate g = gate_raar(0.f);
-  spe::Ctx c = make_ctx(e, first, count);
-  auto trial = [&](int wc, int wr, float* ms) -> int {
+  auto trial_s = [&](int wc, int wr, int chunk, int lanes, float* ms) -> int {
     float t[3];
     for (int r = 0; r < 3; ++r) {
       CK(cudaMemcpyAsync(e->rho + (size_t)first * e->npix, save, bytes, cudaMemcpyDeviceToDevice, e->st), "restore");
       CK(cudaEventRecord(a, e->st), "event");
-      CK(e->ops->iterate(c, 1, iterations, 0.87f, g, wc, wr), "autotune iteration");
+      int rc2 = run_iterations(e, first, count, 1, iterations, 0.87f, g, chunk, lanes, wc, wr);
+      if (rc2) return rc2;
       CK(cudaEventRecord(b, e->st), "event");
       CK(cudaEventSynchronize(b), "event");
       CK(cudaEventElapsedTime(&t[r], a, b), "event");
@@ -653,6 +725,7 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
     *ms = t[1];
     return SPE_OK;
   };
+  auto trial = [&](int wc, int wr, float* ms) { return trial_s(wc, wr, 0, 1, ms); };
   int wcs[8], wrs[8];
   const int nc = e->ops->col_widths(wcs), nr = e->ops->row_widths(wrs);
   int best_c = e->tile_cols > 0 ? e->tile_cols : e->ops->default_cols;
@@ -675,6 +748,25 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
       best_r = wrs[i];
     }
   }
+  // then the schedule: whole range, or L2-sized blocks on one or two lanes
+  int best_chunk = 0, best_lanes = 1;
+  if (!rc) {
+    float ms = 0.f;
+    rc = trial_s(best_c, best_r, 0, 1, &ms);
+    best = ms;
+    const size_t per_ind = e->npix * (2 * sizeof(float2) + sizeof(int));  // rho, T, S
+    const size_t l2 = l2_bytes(e->dev);
+    for (int lanes = 1; !rc && lanes <= 2; ++lanes)
+      for (int chunk : {32, 24, 16, 12, 8, 4}) {
+        if (chunk >= count || (size_t)chunk * lanes * per_ind > l2) continue;
+        if ((rc = trial_s(best_c, best_r, chunk, lanes, &ms))) break;
+        if (ms < best * 0.98f) {
+          best = ms;
+          best_chunk = chunk;
+          best_lanes = lanes;
+        }
+      }
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
@@ -682,6 +774,8 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
   CK(cudaStreamSynchronize(e->st), "synchronize");
   e->tile_cols = best_c;
   e->tile_rows = best_r;
+  e->chunk = best_chunk;
+  e->lanes = best_lanes;
   if (cols) *cols = best_c;
   if (rows) *rows = best_r;
   return SPE_OK;

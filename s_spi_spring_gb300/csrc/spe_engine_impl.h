@@ -38,6 +38,13 @@ struct spe_engine {
   void* work = nullptr;        // grow-only scratch of the population ops
   size_t work_bytes = 0;
   int tile_cols = 0, tile_rows = 0;  // iteration kernel tile widths (0: defaults)
+  // iteration schedule: the population runs in blocks of `chunk` individuals
+  // (0: the whole range), each block through all its iterations before the
+  // next, so that a block's working set stays in L2; with lanes = 2 two
+  // blocks run concurrently on two streams, each kernel on half the SMs
+  int chunk = 0, lanes = 1;
+  cudaStream_t lane2 = nullptr;          // second lane (created on first use)
+  cudaEvent_t fork = nullptr, join = nullptr, phase = nullptr;
 };
 
 
@@ -54,6 +61,8 @@ size_t region(spe_engine* e);
 int reduce(spe_engine* e, const double* part, int count, int tpi, int k, int is_max, int slot);
 int reduce_peak(spe_engine* e, const double* part, int count, int slot);
 int fetch_red(spe_engine* e, int count);
+int run_iterations(spe_engine* e, int first, int count, int upd, int iters, float beta, const spe::Gate& g, int chunk,
+                   int lanes, int wc, int wr);
 }  // namespace spe_detail
 
 #define CK(call, what)                                 \

@@ -55,6 +55,8 @@ struct Ctx {
   const float2* tw;     // exp(+2 pi i m / n), m < n
   double* partials;     // per-CTA reduction slots
   double* red;          // per-individual reduced values, count * 4 * slots
+  int grid_div;         // persistent kernels use 1/grid_div of the resident CTAs (<= 1: all)
+  cudaEvent_t mark;     // if set, recorded after the first column pass of an iteration call
 };
 
 // Phase gate (see phase_out in spe_kernels.cuh): float thresholds of

@@ -314,6 +314,20 @@ __global__ void k_scale_items(float2* __restrict__ rho, const float* __restrict_
     r[i] = make_float2(r[i].x * f, r[i].y * f);
 }
 
+// individual dst_first+blockIdx.y <- individual src[blockIdx.y] (density and
+// support, 16-byte vectors; npix is a multiple of 4)
+__global__ void k_gather(float2* __restrict__ rho, int* __restrict__ S, const int* __restrict__ src, int dst_first,
+                         size_t npix) {
+  const size_t from = (size_t)src[blockIdx.y] * npix, to = (size_t)(dst_first + blockIdx.y) * npix;
+  const float4* rs = reinterpret_cast<const float4*>(rho + from);
+  float4* rd = reinterpret_cast<float4*>(rho + to);
+  const int4* ss = reinterpret_cast<const int4*>(S + from);
+  int4* sd = reinterpret_cast<int4*>(S + to);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix / 2; i += stride) rd[i] = rs[i];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npix / 4; i += stride) sd[i] = ss[i];
+}
+
 }  // namespace spe
 
 namespace {
@@ -600,6 +614,26 @@ int spe_copy(spe_engine* e, int src, int dst, int count) {
   CK(cudaMemcpyAsync(e->S + (size_t)dst * e->npix, e->S + (size_t)src * e->npix,
                      (size_t)count * e->npix * sizeof(int), cudaMemcpyDeviceToDevice, e->st),
      "copy support");
+  return SPE_OK;
+}
+
+int spe_gather(spe_engine* e, const int* src, int count, int dst_first) {
+  int rc = check_range(e, dst_first, count);
+  if (rc) return rc;
+  if (count == 0) return SPE_OK;
+  if (!src) return fail(SPE_ERR_INVALID, "null slot list");
+  for (int k = 0; k < count; ++k) {
+    if (src[k] < 0 || src[k] >= e->cap) return fail(SPE_ERR_INVALID, "slot %d outside capacity %d", src[k], e->cap);
+    if (src[k] >= dst_first && src[k] < dst_first + count)
+      return fail(SPE_ERR_INVALID, "source slot %d inside the destination range", src[k]);
+  }
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  if ((rc = ensure_work(e, (size_t)count * sizeof(int) + 256))) return rc;
+  int* d_src = static_cast<int*>(e->work);
+  CK(cudaMemcpyAsync(d_src, src, (size_t)count * sizeof(int), cudaMemcpyHostToDevice, e->st), "slot list");
+  const unsigned bx = (unsigned)std::max<size_t>(1, std::min<size_t>(152 * 4 / std::max(count, 1) + 1, e->npix / 1024));
+  spe::k_gather<<<dim3(bx, count), 256, 0, e->st>>>(e->rho, e->S, d_src, dst_first, e->npix);
+  CK(cudaGetLastError(), "gather");
   return SPE_OK;
 }
 

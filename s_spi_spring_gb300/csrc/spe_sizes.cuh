@@ -97,6 +97,12 @@ int resident_ctas(K kern, int threads, size_t smem, int* cache) {
   return cache[dev];
 }
 
+// the resident CTAs a persistent launch takes when `div` kernels share the GPU
+inline int share(int slots, int div) {
+  const int s = div > 1 ? slots / div : slots;
+  return s < 1 ? 1 : s;
+}
+
 template <int N, int W>
 cudaError_t launch_cols_project(const Ctx& c) {
   using P = ColCfg<N, W>;
@@ -106,7 +112,7 @@ cudaError_t launch_cols_project(const Ctx& c) {
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
-  const int slots = resident_ctas(kern, P::NT, P::SMEM, resident);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
   kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
   return cudaGetLastError();
@@ -121,7 +127,7 @@ cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
-  const int slots = resident_ctas(kern, P::NT, P::SMEM, resident);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
   kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.rho, c.S, c.first, c.count, scale, beta, g, c.tw);
   return cudaGetLastError();
@@ -198,9 +204,11 @@ struct SizeImpl {
     it.g = g;
     for (int i = 0; i < iters; ++i) {
       SPE_TRY(launch_cols_w<N>(c, wc));
+      if (i == 0 && c.mark) SPE_TRY(cudaEventRecord(c.mark, c.st));
       SPE_TRY((launch_rows_w<N, UPD>(c, wr, scale(), beta, g)));
     }
     SPE_TRY(launch_cols_w<N>(c, wc));
+    if (iters == 0 && c.mark) SPE_TRY(cudaEventRecord(c.mark, c.st));
     OpRowsFinal fin;
     fin.first = c.first;
     fin.partials = nullptr;

@@ -180,6 +180,7 @@ def test_initialize_pop_then_copy_slots():
     eng = _lib.Engine(n, 0)
     eng.set_amplitudes(_lib.prepare_pattern(I, (-1, -1), True))
     eng.seed(9)
+    eng.reserve(12)
     eng.initialize_pop(2, 4, 50, (5.0, 25.0), (2, 9), (0.5, 0.5), (0.5, 1.5), 0.3)
     d0, s0 = eng.download(2, 4)
     eng.copy(2, 8, 4)

@@ -55,3 +55,37 @@ def test_autotune_restores_population_and_picks_compiled_widths():
     assert np.array_equal(got, dens) and np.array_equal(gs, S)
     e.set_tiles(0, 0)
     assert e.tiles() != (0, 0)
+
+
+@pytest.mark.parametrize("alg", ["raar", "hio", "er"])
+def test_schedules_bit_identical(alg):
+    """Blocks of individuals on one or two lanes: the same kernels on the
+    same individuals, so the results are bit-identical to the whole-range
+    call; ragged last blocks and a block larger than the range included."""
+    n, P = 256, 11
+    e, dens, S = engine(n, P, seed=7)
+    run = {"raar": lambda: e.raar(1, P - 1, 4, 0.87, 0.0), "hio": lambda: e.hio(1, P - 1, 4, 0.9, 0.0),
+           "er": lambda: e.er(1, P - 1, 4, 0.0)}[alg]
+    ref = None
+    for chunk, lanes in [(0, 1), (3, 1), (4, 2), (1, 2), (7, 2), (32, 2)]:
+        e.set_schedule(chunk, lanes)
+        assert e.schedule() == (chunk, lanes)
+        e.upload(0, dens, S)
+        run()
+        got, _ = e.download(0, P)
+        assert np.array_equal(got[0].view(np.uint32), dens[0].view(np.uint32))  # slot 0 untouched
+        if ref is None:
+            ref = got
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (chunk, lanes)
+    with pytest.raises(_lib.EngineError):
+        e.set_schedule(4, 3)
+
+
+def test_autotune_schedule_fits_l2():
+    n, P = 512, 32
+    e, dens, S = engine(n, P, seed=5)
+    e.autotune(0, P, iterations=4)
+    chunk, lanes = e.schedule()
+    assert lanes in (1, 2) and (chunk == 0 or chunk * lanes * n * n * 20 <= 129 * 2**20)
+    got, _ = e.download(0, P)
+    assert np.array_equal(got, dens)
