@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
+    ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
     ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
     ap.add_argument("--schedule", default="", help="chunk,lanes iteration schedule (implies --no-tune)")
@@ -59,6 +60,23 @@ def parse():
 
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def max_over_ranks(ms: float, world: int, device: str) -> float:
+    """The slowest rank's time (replicas: every rank runs its own
+    population; the job ends with the last one)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank_step: float, world: int, ms_step: float) -> float:
+    """Units all ranks processed per second of the slowest rank."""
+    return units_per_rank_step * world / (ms_step / 1e3)
 
 
 def workload(seed=1):
@@ -70,7 +88,10 @@ def workload(seed=1):
 
 
 class ClockSampler:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling (every 20 ms) around the timed region: started
+    before it, waits for the first sample, and summarises the samples taken
+    between mark_start() and mark_end() (the nearest ones when the region is
+    shorter than the sampling period)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -79,22 +100,33 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (monotonic time, line)
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.monotonic() + 5.0
+            while not self.lines and time.monotonic() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def mark_start(self):
+        self.t0 = time.monotonic()
+
+    def mark_end(self):
+        self.t1 = time.monotonic()
+        time.sleep(0.05)  # the sample after the region
 
     def __exit__(self, *exc):
         if self.proc:
@@ -104,10 +136,19 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+    def _window(self):
+        if self.t0 is None or self.t1 is None:
+            return [ln for _, ln in self.lines]
+        inside = [ln for t, ln in self.lines if self.t0 <= t <= self.t1]
+        if inside:
+            return inside
+        near = sorted(self.lines, key=lambda x: min(abs(x[0] - self.t0), abs(x[0] - self.t1)))
+        return [ln for _, ln in near[:2]]
+
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self._window():
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -181,6 +222,44 @@ def plain_gpu(args, A, dens, S, local, eng):
                                    "max_abs_diff": float(np.max(np.abs(np.array(r_eng) - np.array(r_plain))))}}
 
 
+def memetic(args, local, tiles, sched):
+    """The population workload's generation loop (shrink-wrap, alignment,
+    average, crossover, RAAR/ER sequences on parents and children,
+    replacement) through the drop-in Solver with device-resident
+    individuals: seconds per generation and the iterations it ran."""
+    import numpy as np
+    import torch
+    from s_spi_spring_gb300 import synthetic
+    from s_spi_spring_gb300.memetic import MemeticRun, MemeticSettings
+    from s_spi_spring_gb300.spring_core.phase_retrieval import Solver
+    I, _, _ = synthetic.polygon_pattern(seed=1, n=N, diameter=120.0, photons=1e7, stop_radius=8, gap=4, stripes=2)
+    st = MemeticSettings(generations=10, popsize=POP, alg="RAAR", it=args.iters, beta=BETA, it_ER=20, it_eval=20,
+                         sigma=3.0, threshold=0.1)
+    sol = Solver(I, gpus=[local], seed=42)
+    sol.engine.set_tiles(*tiles)
+    sol.engine.set_schedule(*sched)
+    recs = sol.InitializePop(POP, 128, itemsize=[128 * 0.2, 128 * 0.9], nitems=[2, 8], exponent=[0.5, 0.5],
+                             scaling=[0.5, 1.5], phaserange=0)
+    run = MemeticRun(sol, recs, st)
+    run.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    iters = 0
+    for _ in range(args.memetic_gens):
+        seq = run.algman.sequence(run.generation + 1, area=[1, 1])
+        per_pop = sum(int(p[0]) for name, p in seq if name in ("HIO", "RAAR", "ER"))
+        iters += 2 * POP * per_pop  # parents and children
+        run.step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"generations": args.memetic_gens, "s_per_generation": round(dt / args.memetic_gens, 4),
+            "iter_ind_per_s": round(iters / dt, 1), "best_error": [round(h["best"], 6) for h in run.history],
+            "replaced": [h["replaced"] for h in run.history],
+            "what": "MPR generation (SW, Reshift, GetAverage, Crossover, Sequence x2, replacement) through the "
+                    "Solver front end, individuals resident on the device; iterations counted over HIO/RAAR/ER "
+                    "ops of both sequences"}
+
+
 def run_engine(args):
     import torch
     from s_spi_spring_gb300 import _lib
@@ -213,22 +292,19 @@ def run_engine(args):
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
+        clocks.mark_start()
         ev0.record(stream)
         for _ in range(args.steps):
             eng.raar(0, POP, args.iters, BETA, 0.0)
         ev1.record(stream)
         ev1.synchronize()
+        clocks.mark_end()
     torch.cuda.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world, f"cuda:{local}")
     ms_step = ms / args.steps
     units_per_step = POP * args.iters
-    value = units_per_step * world / (ms_step / 1e3)
+    value = whole_job_rate(units_per_step, world, ms_step)
 
     # ---- per-iteration time of the fused iteration kernels (row + column pass):
     # a call of k iterations minus a call of 0 iterations, on the same stream
@@ -303,7 +379,7 @@ def run_engine(args):
                      "kernel": "fused iteration (column pass + row pass), per iteration",
                      "alg_bytes_per_launch": alg_bytes, "ms_per_iteration": round(t_iter_ms, 5),
                      "peak_source": peak_kind},
-        "gpu_launches": args.steps * (2 * args.iters + 3),
+        "gpu_launches": args.steps * (2 * args.iters + 3) * (-(-POP // sched[0]) if sched[0] > 0 else 1),
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_plain:
@@ -312,6 +388,11 @@ def run_engine(args):
             out["plain_gpu"]["fused_over_plain"] = round(value / world / out["plain_gpu"]["value"], 3)
         except Exception as ex:
             out["plain_gpu"] = {"error": str(ex)[:200]}
+    if rank == 0 and args.memetic_gens > 0:
+        try:
+            out["memetic"] = memetic(args, local, tiles, sched)
+        except Exception as ex:
+            out["memetic"] = {"error": str(ex)[:200]}
     if rank == 0 and not args.no_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline(args.cpu_sample_s)

@@ -656,7 +656,7 @@ int spe_set_tiles(spe_engine* e, int cols, int rows) {
   if (!e) return fail(SPE_ERR_INVALID, "null engine");
   int w[8];
   auto ok = [&](int v, int (*f)(int*)) {
-    if (v <= 0) return true;
+    if (v == 0) return true;
     const int k = f(w);
     for (int i = 0; i < k; ++i)
       if (w[i] == v) return true;
@@ -686,7 +686,7 @@ int spe_get_schedule(spe_engine* e, int* chunk, int* lanes) {
 
 int spe_get_tiles(spe_engine* e, int* cols, int* rows) {
   if (!e || !cols || !rows) return fail(SPE_ERR_INVALID, "null argument");
-  *cols = e->tile_cols > 0 ? e->tile_cols : e->ops->default_cols;
+  *cols = e->tile_cols != 0 ? e->tile_cols : e->ops->default_cols;
   *rows = e->tile_rows > 0 ? e->tile_rows : e->ops->default_rows;
   return SPE_OK;
 }
@@ -728,7 +728,7 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
   auto trial = [&](int wc, int wr, float* ms) { return trial_s(wc, wr, 0, 1, ms); };
   int wcs[8], wrs[8];
   const int nc = e->ops->col_widths(wcs), nr = e->ops->row_widths(wrs);
-  int best_c = e->tile_cols > 0 ? e->tile_cols : e->ops->default_cols;
+  int best_c = e->tile_cols != 0 ? e->tile_cols : e->ops->default_cols;
   int best_r = e->tile_rows > 0 ? e->tile_rows : e->ops->default_rows;
   float best = 1e30f;
   for (int i = 0; i < nc; ++i) {

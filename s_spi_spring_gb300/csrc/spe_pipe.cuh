@@ -212,4 +212,176 @@ __global__ void __launch_bounds__(RowCfg<N, W>::NT, RowCfg<N, W>::MINB)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Column pass with two columns per thread.  Thread (pair h, j) holds the E
+// elements of columns 2h and 2h+1 at the same positions, so every exchange
+// moves one 16-byte (float4) element pair, each twiddle loaded serves both
+// columns, and the two radix passes interleave (two independent dependency
+// chains per thread).  Used where E <= 8 (sizes up to 512).
+// ---------------------------------------------------------------------------
+
+// pair layout: element pair (l, h) of WP pairs per row; row l moves to
+// l ^ ((l >> 3) & (8/WP - 1)) so that the rows a group of 8 lanes touches in a
+// Stockham store (l = 8j + q, consecutive j) land in different 16-byte bank
+// groups; reads (consecutive l) are conflict free with or without it
+template <int L, int WP>
+struct LayPair {
+  static constexpr int SIZE = L * WP;
+  static __device__ __forceinline__ int idx(int l, int h) {
+    if (WP >= 8) return l * WP + h;
+    return (l ^ ((l >> 3) & (8 / WP - 1))) * WP + h;
+  }
+};
+
+template <int N, int WP>
+struct PairCfg {  // column pass, 2*WP columns per tile
+  static constexpr int TPT = Plan<N>::TPT;
+  static constexpr int E = Elems<N>::value;
+  static constexpr int W = 2 * WP;
+  static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
+  static constexpr int NT = WP * TPT;
+  static constexpr int C_T = align128(N * WP * 16);
+  static constexpr int C_A = align128(N * W * 4);
+  static constexpr int STAGE = C_T + C_A;
+  static constexpr size_t SMEM = (size_t)TWB + 2 * STAGE;
+  static constexpr int MINB_RAW = 65536 / (NT * 128);
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
+};
+
+template <int L, int TPT, int S, class Lay, int P, int NS>
+__device__ __forceinline__ void fft_pass_pair(float2* a, float2* b, float4* __restrict__ buf,
+                                              const float2* __restrict__ tw, int h, int j) {
+  using Rad = typename Plan<L>::R;
+  constexpr int R = Rad::value[P];
+  constexpr int NB = L / R;
+  constexpr int U = NB / TPT;
+  static_assert(NB % TPT == 0, "butterflies must divide evenly over the threads");
+  constexpr int OFF = TwiddleTable<L>::offset(P);
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int bb = j + TPT * u;
+    const int k = (NS == 1) ? 0 : (bb % NS);
+    if constexpr (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        float2 w = tw[OFF + (r - 1) * NS + k];
+        if (S < 0) w.y = -w.y;
+        a[u * R + r] = cmul(a[u * R + r], w);
+        b[u * R + r] = cmul(b[u * R + r], w);
+      }
+    }
+    dft<R, S>(a + u * R);
+    dft<R, S>(b + u * R);
+  }
+  if constexpr (P + 1 < Rad::count) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int bb = j + TPT * u;
+      const int k = (NS == 1) ? 0 : (bb % NS);
+      const int base = (bb / NS) * NS * R + k;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        const float2 x = a[u * R + q], y = b[u * R + q];
+        buf[Lay::idx(base + q * NS, h)] = make_float4(x.x, x.y, y.x, y.y);
+      }
+    }
+    __syncthreads();
+    constexpr int R2 = Rad::value[P + 1];
+    constexpr int NB2 = L / R2;
+    constexpr int U2 = NB2 / TPT;
+    static_assert(U2 * R2 == U * R, "every pass must keep E elements per thread");
+#pragma unroll
+    for (int u = 0; u < U2; ++u) {
+      const int bb = j + TPT * u;
+#pragma unroll
+      for (int r = 0; r < R2; ++r) {
+        const float4 t4 = buf[Lay::idx(bb + r * NB2, h)];
+        a[u * R2 + r] = make_float2(t4.x, t4.y);
+        b[u * R2 + r] = make_float2(t4.z, t4.w);
+      }
+    }
+    __syncthreads();
+    fft_pass_pair<L, TPT, S, Lay, P + 1, NS * R>(a, b, buf, tw, h, j);
+  }
+}
+
+template <int L, class Lay, int S>
+__device__ __forceinline__ void fft_pair(float2* a, float2* b, float4* buf, const float2* tw, int h, int j) {
+  using Rad = typename Plan<L>::R;
+  static_assert(Rad::value[0] == Rad::value[Rad::count - 1], "first and last radix must match");
+  fft_pass_pair<L, Plan<L>::TPT, S, Lay, 0, 1>(a, b, buf, tw, h, j);
+}
+
+// column pass, two columns per thread: T -> FFT+ (y) -> P_M -> FFT- (y) -> T
+template <int N, int WP>
+__global__ void __launch_bounds__(PairCfg<N, WP>::NT, PairCfg<N, WP>::MINB)
+    k_cols_pair(float2* __restrict__ T, const float* __restrict__ A, int first, int count,
+                const float2* __restrict__ twg) {
+  using C = PairCfg<N, WP>;
+  constexpr int NT = C::NT, E = C::E, W = C::W, TPI = N / W;
+  static_assert(W % 4 == 0, "amplitude rows are copied in 16-byte chunks");
+  using Lay = LayPair<N, WP>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  float2* tw = reinterpret_cast<float2*>(sm);
+  unsigned char* stages = sm + C::TWB;
+  load_twiddles<N>(tw, twg, NT);
+  const int t = threadIdx.x;
+  const int h = t % WP, j = t / WP;
+  const int ntiles = count * TPI;
+
+  auto stage_tile = [&](int tile, int s) {
+    const int p = first + tile / TPI;
+    const int x0 = (tile % TPI) * W;
+    float4* sT = reinterpret_cast<float4*>(stages + s * C::STAGE);
+    float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
+    const float2* gT = T + (size_t)p * N * N + x0;
+    for (int q = t; q < N * WP; q += NT) {
+      const int y = q / WP, hh = q - y * WP;
+      cp_async16(&sT[Lay::idx(y, hh)], gT + (size_t)y * N + 2 * hh);
+    }
+    for (int q = t; q < N * W / 4; q += NT) {
+      const int y = q / (W / 4), hh = q - y * (W / 4);
+      cp_async16(&sA[y * W + 4 * hh], A + (size_t)y * N + x0 + 4 * hh);
+    }
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) stage_tile(tile, 0);
+  cp_async_commit();
+  for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) stage_tile(nxt, (k + 1) & 1);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    const int s = k & 1;
+    float4* sT = reinterpret_cast<float4*>(stages + s * C::STAGE);
+    const float* sA = reinterpret_cast<const float*>(stages + s * C::STAGE + C::C_T);
+    const int p = first + tile / TPI;
+    const int x = (tile % TPI) * W + 2 * h;
+    float2 a[E], b[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const float4 t4 = sT[Lay::idx(elem_pos<N>(e, j), h)];
+      a[e] = make_float2(t4.x, t4.y);
+      b[e] = make_float2(t4.z, t4.w);
+    }
+    __syncthreads();  // the stage's T region becomes the exchange buffer
+    fft_pair<N, Lay, +1>(a, b, sT, tw, h, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int y = elem_pos<N>(e, j);
+      const float2 am = *reinterpret_cast<const float2*>(&sA[y * W + 2 * h]);
+      a[e] = project(a[e], am.x);
+      b[e] = project(b[e], am.y);
+    }
+    fft_pair<N, Lay, -1>(a, b, sT, tw, h, j);
+    float2* gT = T + (size_t)p * N * N + x;
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      *reinterpret_cast<float4*>(gT + (size_t)elem_pos<N>(e, j) * N) = make_float4(a[e].x, a[e].y, b[e].x, b[e].y);
+    __syncthreads();  // stage s is refilled by the next iteration's prefetch
+  }
+}
+
 }  // namespace spe

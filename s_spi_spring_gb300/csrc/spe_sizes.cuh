@@ -71,6 +71,12 @@ constexpr bool row_ok() {
   return W <= N && N % W == 0 && RowCfg<N, W>::NT % 32 == 0 && RowCfg<N, W>::NT <= 1024 &&
          RowCfg<N, W>::SMEM <= kMaxSmem;
 }
+// two-columns-per-thread variants (registers for 2E elements): E <= 8 only
+template <int N, int W>
+constexpr bool pair_ok() {
+  return W % 4 == 0 && W <= N && N % W == 0 && Elems<N>::value <= 8 && PairCfg<N, W / 2>::NT % 32 == 0 &&
+         PairCfg<N, W / 2>::NT <= 1024 && PairCfg<N, W / 2>::SMEM <= kMaxSmem;
+}
 constexpr int kColWidths[3] = {4, 8, 16};
 constexpr int kRowWidths[5] = {1, 2, 4, 8, 16};
 
@@ -133,9 +139,29 @@ cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
   return cudaGetLastError();
 }
 
+template <int N, int W>
+cudaError_t launch_cols_pair(const Ctx& c) {
+  using P = PairCfg<N, W / 2>;
+  auto kern = k_cols_pair<N, W / 2>;
+  static unsigned long long configured = 0ull;
+  static int resident[64] = {0};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / W);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
+  const int grid = tiles < slots ? tiles : slots;
+  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
+  return cudaGetLastError();
+}
+
+// column-pass variant code: W > 0 one column per thread, W columns per tile;
+// W < 0 two columns per thread, -W columns per tile
 template <int N>
 cudaError_t launch_cols_w(const Ctx& c, int w) {
   switch (w) {
+    case -4: if constexpr (pair_ok<N, 4>()) return launch_cols_pair<N, 4>(c); break;
+    case -8: if constexpr (pair_ok<N, 8>()) return launch_cols_pair<N, 8>(c); break;
+    case -16: if constexpr (pair_ok<N, 16>()) return launch_cols_pair<N, 16>(c); break;
     case 4: if constexpr (col_ok<N, 4>()) return launch_cols_project<N, 4>(c); break;
     case 8: if constexpr (col_ok<N, 8>()) return launch_cols_project<N, 8>(c); break;
     case 16: if constexpr (col_ok<N, 16>()) return launch_cols_project<N, 16>(c); break;
@@ -220,7 +246,7 @@ struct SizeImpl {
 
   // wc / wr: tile widths of the column / row pass (<= 0: defaults)
   static cudaError_t iterate(const Ctx& c, int upd, int iters, float beta, Gate g, int wc, int wr) {
-    if (wc <= 0) wc = DefaultTiles<N>::cols;
+    if (wc == 0) wc = DefaultTiles<N>::cols;
     if (wr <= 0) wr = DefaultTiles<N>::rows;
     switch (upd) {
       case 0: return iterate_t<UPD_HIO>(c, iters, beta, g, wc, wr);
@@ -231,6 +257,9 @@ struct SizeImpl {
 
   static int col_widths(int* out) {
     int k = 0;
+    if constexpr (pair_ok<N, 4>()) out[k++] = -4;
+    if constexpr (pair_ok<N, 8>()) out[k++] = -8;
+    if constexpr (pair_ok<N, 16>()) out[k++] = -16;
     if constexpr (col_ok<N, 4>()) out[k++] = 4;
     if constexpr (col_ok<N, 8>()) out[k++] = 8;
     if constexpr (col_ok<N, 16>()) out[k++] = 16;

@@ -37,8 +37,11 @@ class RoundTripSolver(Solver):
         return super()._stage(recs)
 
     def _resident(self, r):
-        r._sync_host()
-        r._unbind()
+        # individuals of the list just staged (host copy current) stay; any
+        # other (the average, a reference) goes through the host
+        if not (r._home is not None and r._home[0] is self and r._dev_ok and r._host_ok):
+            r._sync_host()
+            r._unbind()
         return super()._resident(r)
 
 

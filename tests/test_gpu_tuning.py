@@ -1,8 +1,9 @@
 """Tile-width variants of the iteration kernels and the autotuner.
 
-Every compiled tile width performs the same per-element arithmetic, so all
-variants must give bit-identical results; the autotuner must leave the
-population as it found it."""
+Every compiled tile width -- including the column pass that keeps two
+columns per thread (negative widths) -- performs the same per-element
+arithmetic, so all variants must give bit-identical results; the autotuner
+must leave the population as it found it."""
 import itertools
 
 import numpy as np
@@ -23,13 +24,13 @@ def engine(n, P, seed=0):
     return e, dens, S
 
 
-@pytest.mark.parametrize("n", [128, 512, 1024])
+@pytest.mark.parametrize("n", [64, 128, 256, 384, 512, 1024])
 def test_all_tile_widths_bit_identical(n):
     P = 3
     e, dens, S = engine(n, P)
     ref = None
     tried = 0
-    for wc, wr in itertools.product([4, 8, 16], [1, 2, 4, 8, 16]):
+    for wc, wr in itertools.product([4, 8, 16, -4, -8, -16], [1, 2, 4, 8, 16]):
         try:
             e.set_tiles(wc, wr)
         except _lib.EngineError:
