@@ -103,6 +103,16 @@ int spe_get_stream(spe_engine* e, void** cuda_stream);
 int spe_set_amplitudes(spe_engine* e, const float* amplitudes);
 int spe_get_amplitudes(spe_engine* e, float* amplitudes);
 
+/* Several patterns of the engine's size in one population (no reference
+ * counterpart; the reference builds one Solver per pattern): amplitudes
+ * holds npatterns arrays of n x n, and slot p uses pattern
+ * p / individuals_per_pattern.  Iterations, shrink-wrap, evaluation,
+ * initialisation and the loss use each slot's own pattern; alignment,
+ * averages and crossover act on ranges within one pattern (others are
+ * rejected).  spe_set_amplitudes returns to a single shared pattern;
+ * spe_get_amplitudes reads pattern 0. */
+int spe_set_amplitudes_batch(spe_engine* e, const float* amplitudes, int npatterns, int individuals_per_pattern);
+
 /* Population capacity in individuals (device memory for density, support
  * and scratch).  Existing contents up to min(old, new) are kept. */
 int spe_reserve(spe_engine* e, int capacity);
@@ -229,6 +239,39 @@ int spe_crossover_draws(uint32_t seed, int count, const int32_t* order, float su
  * the engine's pattern size are accepted. */
 int spe_set_tiles(spe_engine* e, int cols, int rows);
 int spe_get_tiles(spe_engine* e, int* cols, int* rows);
+
+/* Far-field loss and its gradient (gradient refinement; no reference
+ * counterpart).  For items k < count of the caller's DEVICE arrays
+ * density (complex64, count*n*n) and support (int32), with F = the
+ * iteration's transform of support*density (exponent +i, unnormalised) and
+ * the engine's amplitudes A, summed over the known pixels (A >= 0):
+ *   SPE_LOSS_AMPLITUDE: L = sum (|F| - A)^2
+ *   SPE_LOSS_POISSON:   L = sum |F|^2 - A^2 log(|F|^2 + eps)
+ * loss_out (device, count doubles, may be NULL) receives L per item;
+ * grad_out (device, complex64 count*n*n, may be NULL) receives
+ * grad_scale[k] * 2 dL/dconj(density) (grad_scale: device, count floats, or
+ * NULL for 1): support * FFT-(2 dL/dconj F), the gradient convention of
+ * complex autograd.  The transform is recomputed, nothing is stored between
+ * the loss and the gradient.  Runs on the engine's stream; the engine's
+ * population capacity grows to `count` for scratch. */
+enum { SPE_LOSS_AMPLITUDE = 0, SPE_LOSS_POISSON = 1 };
+int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
+                  double* loss_out, void* grad_out, const float* grad_scale);
+
+/* CUDA graphs of engine calls (no reference counterpart).  Between
+ * spe_graph_begin(stream) and spe_graph_end(stream, &g), asynchronous engine
+ * calls of one or more engines whose stream (spe_set_stream) is `stream` are
+ * recorded instead of run: HIO / RAAR / ER, SW with a relative threshold,
+ * copies and gathers.  Calls that return results to the host (evaluate,
+ * sequences with metrics, downloads, SWA, crossover, alignment) must not be
+ * captured.  Make one uncaptured call of each recorded kind first: kernels
+ * are configured on their first launch.  spe_graph_launch replays the whole
+ * recording as one graph launch on any stream. */
+typedef struct spe_graph spe_graph;
+int spe_graph_begin(void* stream);
+int spe_graph_end(void* stream, spe_graph** out);
+int spe_graph_launch(spe_graph* g, void* stream);
+int spe_graph_destroy(spe_graph* g);
 
 /* Iteration schedule (no reference counterpart; the reference runs one
  * individual per context): HIO / RAAR / ER calls process the range in blocks

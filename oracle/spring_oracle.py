@@ -784,3 +784,37 @@ def initialize_pop(A, rng, count, support_size, itemsize, nitems, exponent, scal
         norm_new = np.sum(A[known].astype(np.float64) ** 2)
         dens[k] = (dens[k] * f32(np.sqrt(f32(norm_new) / f32(norm)) * sc)).astype(np.complex64)
     return dens, supp
+
+
+# ----------------------------------------------------------------------------
+# Far-field loss and gradient (gradient refinement; no reference counterpart)
+# ----------------------------------------------------------------------------
+def farfield_loss_grad(rho, S, A, loss="amplitude", eps=0.0):
+    """Float64 loss and gradient of one individual.  F = ft(S*rho) (the
+    iteration's transform); over the known pixels A >= 0:
+    amplitude L = sum (|F|-A)^2, Poisson L = sum |F|^2 - A^2 log(|F|^2+eps).
+    Returns (L, G) with G = 2 dL/dconj(rho) = S * adjoint(2 dL/dconj(F)),
+    the adjoint of ft being the unnormalised transform of exponent -i,
+    ``N*N*ift``.  The convention is that of complex autograd: a step
+    rho - lr*G descends."""
+    rho = np.asarray(rho, dtype=np.complex128)
+    Sm = (np.asarray(S) > 0).astype(np.float64)
+    A = np.asarray(A, dtype=np.float64)
+    F = ft(rho * Sm)
+    known = A >= 0
+    m2 = np.abs(F) ** 2
+    if loss == "amplitude":
+        m = np.sqrt(m2)
+        d = m - A
+        L = float(np.sum((d ** 2)[known]))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            gF = np.where(known & (m > 0), 2.0 * d / np.where(m > 0, m, 1.0), 0.0) * F
+    elif loss == "poisson":
+        I = A ** 2
+        L = float(np.sum((m2 - I * np.log(m2 + eps))[known]))
+        gF = np.where(known, 2.0 * (1.0 - I / (m2 + eps)), 0.0) * F
+    else:
+        raise ValueError(loss)
+    n0, n1 = rho.shape
+    G = Sm * (np.fft.fft2(gF))  # unnormalised exponent -i: the adjoint of ft
+    return L, G

@@ -18,6 +18,7 @@ _lib = None
 
 SPE_OK = 0
 SPE_OP_HIO, SPE_OP_RAAR, SPE_OP_ER, SPE_OP_SW, SPE_OP_SWA = range(5)
+SPE_LOSS_AMPLITUDE, SPE_LOSS_POISSON = 0, 1
 
 # Every symbol the header declares, with (restype, argtypes).
 _vp = C.c_void_p
@@ -76,7 +77,61 @@ SIGNATURES = {
     "spe_initialize_pop": (_i, [_vp, _i, _i, _i, _f, _f, _i, _i, _f, _f, _f, _f, _f, _f]),
     "spe_copy": (_i, [_vp, _i, _i, _i]),
     "spe_gather": (_i, [_vp, _ip, _i, _i]),
+    "spe_loss_grad": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp, _vp]),
+    "spe_set_amplitudes_batch": (_i, [_vp, _fp, _i, _i]),
+    "spe_graph_begin": (_i, [_vp]),
+    "spe_graph_end": (_i, [_vp, C.POINTER(_vp)]),
+    "spe_graph_launch": (_i, [_vp, _vp]),
+    "spe_graph_destroy": (_i, [_vp]),
 }
+
+
+class Graph:
+    """A CUDA graph of engine calls recorded on `stream` (a CUDA stream
+    handle): ``with Graph.capture(stream) as g: ...`` then ``g.launch()``."""
+
+    def __init__(self, handle, stream):
+        self.h, self.stream = handle, stream
+
+    @classmethod
+    def capture(cls, stream):
+        return _Capture(stream)
+
+    def launch(self, stream=None):
+        call("spe_graph_launch", self.h, _vp(stream if stream is not None else self.stream))
+
+    def close(self):
+        if self.h:
+            load().spe_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _Capture:
+    def __init__(self, stream):
+        self.stream = stream
+        self.graph = None
+
+    def __enter__(self):
+        call("spe_graph_begin", _vp(self.stream))
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        lib = load()
+        g = _vp()
+        rc = lib.spe_graph_end(_vp(self.stream), C.byref(g))
+        if exc_type is None:
+            if rc != SPE_OK:
+                raise EngineError("spe_graph_end", rc, lib.spe_last_error().decode())
+            self.graph = Graph(g.value, self.stream)
+        elif rc == SPE_OK:
+            lib.spe_graph_destroy(g)
+        return False
 
 
 class EngineError(RuntimeError):
@@ -152,6 +207,12 @@ class Engine:
         amp = np.ascontiguousarray(amp, dtype=np.float32)
         assert amp.shape == (self.n, self.n)
         call("spe_set_amplitudes", self.h, fptr(amp))
+
+    def set_amplitudes_batch(self, amps, individuals_per_pattern):
+        """amps: (npatterns, n, n); slot p uses pattern p // individuals_per_pattern."""
+        amps = np.ascontiguousarray(amps, dtype=np.float32)
+        assert amps.ndim == 3 and amps.shape[1:] == (self.n, self.n)
+        call("spe_set_amplitudes_batch", self.h, fptr(amps), int(amps.shape[0]), int(individuals_per_pattern))
 
     def get_amplitudes(self):
         out = np.empty((self.n, self.n), np.float32)
@@ -257,6 +318,17 @@ class Engine:
 
     def copy(self, src, dst, count):
         call("spe_copy", self.h, int(src), int(dst), int(count))
+
+    def loss_grad(self, density_ptr, support_ptr, count, loss=0, eps=0.0, loss_ptr=0, grad_ptr=0, scale_ptr=0):
+        """Far-field loss / gradient on device arrays given by address."""
+        call("spe_loss_grad", self.h, _vp(density_ptr), _vp(support_ptr), int(count), int(loss), float(eps),
+             _vp(loss_ptr or 0), _vp(grad_ptr or 0), _vp(scale_ptr or 0))
+
+    def population_arrays(self, first, count):
+        """Device addresses of slots [first, first+count): (density, support)."""
+        d, s = self.device_buffers()
+        off = int(first) * self.n * self.n
+        return d + off * 8, s + off * 4
 
     def gather(self, src_slots, dst_first):
         src = np.ascontiguousarray(src_slots, dtype=np.int32)

@@ -205,6 +205,14 @@ int need_amp(spe_engine* e) {
   return SPE_OK;
 }
 
+// every slot of [first, first+count) has a pattern
+int have_patterns(spe_engine* e, int first, int count) {
+  if (e->ipp > 0 && count > 0 && (long long)first + count > (long long)e->npatterns * e->ipp)
+    return fail(SPE_ERR_INVALID, "slots up to %d need %d patterns, %d set", first + count,
+                (first + count + e->ipp - 1) / e->ipp, e->npatterns);
+  return SPE_OK;
+}
+
 spe::Ctx make_ctx(spe_engine* e, int first, int count) {
   spe::Ctx c;
   c.n = e->n;
@@ -222,6 +230,28 @@ spe::Ctx make_ctx(spe_engine* e, int first, int count) {
   c.red = e->red;
   c.grid_div = 1;
   c.mark = nullptr;
+  c.ipp = e->ipp;
+  return c;
+}
+
+int pattern_of_range(spe_engine* e, int first, int count, const float** A) {
+  if (e->ipp <= 0) {
+    *A = e->A;
+    return SPE_OK;
+  }
+  const int pat = first / e->ipp;
+  if (count > 0 && (first + count - 1) / e->ipp != pat)
+    return fail(SPE_ERR_INVALID, "slots [%d, %d) span several patterns (%d individuals per pattern)", first,
+                first + count, e->ipp);
+  if (pat >= e->npatterns) return fail(SPE_ERR_INVALID, "slot %d has no pattern", first);
+  *A = e->A + (size_t)pat * e->npix;
+  return SPE_OK;
+}
+
+spe::Ctx item_ctx(spe_engine* e, int count, const float* A) {
+  spe::Ctx c = make_ctx(e, 0, count);
+  c.A = A;
+  c.ipp = 0;
   return c;
 }
 
@@ -322,6 +352,7 @@ int do_iterate(spe_engine* e, int first, int count, int upd, int iters, float be
   if (rc) return rc;
   if ((rc = need_amp(e))) return rc;
   if (iters < 0) return fail(SPE_ERR_INVALID, "negative iteration count");
+  if ((rc = have_patterns(e, first, count))) return rc;
   if (count == 0) return SPE_OK;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   const spe::Gate g = (upd == 1) ? gate_raar(real) : gate_er(real);
@@ -332,6 +363,7 @@ int do_shrinkwrap(spe_engine* e, int first, int count, float sigma, bool absolut
   int rc = check_range(e, first, count);
   if (rc) return rc;
   if ((rc = need_amp(e))) return rc;
+  if ((rc = have_patterns(e, first, count))) return rc;
   if (count == 0) return SPE_OK;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   // FLOAT sigmaft = FLOAT(npixels)/sigma/M_PI  (gpu_context.cu:935)
@@ -458,6 +490,30 @@ int spe_set_amplitudes(spe_engine* e, const float* amp) {
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   CK(cudaMemcpyAsync(e->A, amp, e->npix * sizeof(float), cudaMemcpyHostToDevice, e->st), "upload amplitudes");
   CK(cudaStreamSynchronize(e->st), "synchronize");
+  e->have_amp = true;
+  e->ipp = 0;
+  e->npatterns = 1;
+  return SPE_OK;
+}
+
+int spe_set_amplitudes_batch(spe_engine* e, const float* amp, int npatterns, int individuals_per_pattern) {
+  if (!e || !amp) return fail(SPE_ERR_INVALID, "null argument");
+  if (npatterns < 1 || individuals_per_pattern < 1)
+    return fail(SPE_ERR_INVALID, "need at least one pattern and one individual per pattern");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  if (npatterns > e->a_cap) {
+    CK(cudaStreamSynchronize(e->st), "synchronize");
+    float* a = nullptr;
+    CK(cudaMalloc(&a, (size_t)npatterns * e->npix * sizeof(float)), "amplitude allocation");
+    cudaFree(e->A);
+    e->A = a;
+    e->a_cap = npatterns;
+  }
+  CK(cudaMemcpyAsync(e->A, amp, (size_t)npatterns * e->npix * sizeof(float), cudaMemcpyHostToDevice, e->st),
+     "upload amplitudes");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  e->npatterns = npatterns;
+  e->ipp = npatterns > 1 ? individuals_per_pattern : 0;
   e->have_amp = true;
   return SPE_OK;
 }
@@ -589,6 +645,7 @@ int spe_evaluate(spe_engine* e, int first, int count, float reality, float realp
   if (rc) return rc;
   if ((rc = need_amp(e))) return rc;
   if (count > 0 && !m) return fail(SPE_ERR_INVALID, "null metrics pointer");
+  if ((rc = have_patterns(e, first, count))) return rc;
   if (count == 0) return SPE_OK;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   spe::Ctx c = make_ctx(e, first, count);
@@ -666,6 +723,76 @@ int spe_set_tiles(spe_engine* e, int cols, int rows) {
     return fail(SPE_ERR_INVALID, "tile widths %d/%d not compiled for size %d", cols, rows, e->n);
   e->tile_cols = cols;
   e->tile_rows = rows;
+  return SPE_OK;
+}
+
+int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
+                  double* loss_out, void* grad_out, const float* grad_scale) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  int rc = need_amp(e);
+  if (rc) return rc;
+  if (count < 0) return fail(SPE_ERR_INVALID, "negative count");
+  if (loss != SPE_LOSS_AMPLITUDE && loss != SPE_LOSS_POISSON) return fail(SPE_ERR_INVALID, "unknown loss %d", loss);
+  if (!(eps >= 0.f)) return fail(SPE_ERR_INVALID, "eps must be >= 0");
+  if (count == 0) return SPE_OK;
+  if (!density || !support) return fail(SPE_ERR_INVALID, "null density or support");
+  if (!loss_out && !grad_out) return SPE_OK;
+  if ((rc = spe_reserve(e, count))) return rc;  // scratch and partials for `count` items
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  spe::Ctx c = make_ctx(e, 0, count);
+  c.rho = static_cast<float2*>(const_cast<void*>(density));
+  c.S = const_cast<int*>(support);
+  CK(e->ops->loss_grad(c, loss, eps, e->partials, static_cast<float2*>(grad_out), grad_scale), "loss kernels");
+  if (loss_out) {
+    if ((rc = reduce(e, e->partials, count, e->ops->tiles_cols, 0, 0, 0))) return rc;
+    CK(cudaMemcpy2DAsync(loss_out, sizeof(double), e->red, 16 * sizeof(double), sizeof(double), count,
+                         cudaMemcpyDeviceToDevice, e->st),
+       "loss copy");
+  }
+  return SPE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CUDA graphs of engine calls
+// ---------------------------------------------------------------------------
+struct spe_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+int spe_graph_begin(void* stream) {
+  if (!stream) return fail(SPE_ERR_INVALID, "capture needs an explicit stream");
+  CK(cudaStreamBeginCapture(static_cast<cudaStream_t>(stream), cudaStreamCaptureModeThreadLocal), "begin capture");
+  return SPE_OK;
+}
+
+int spe_graph_end(void* stream, spe_graph** out) {
+  if (!stream || !out) return fail(SPE_ERR_INVALID, "null argument");
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamEndCapture(static_cast<cudaStream_t>(stream), &g), "end capture");
+  spe_graph* h = new spe_graph();
+  h->graph = g;
+  cudaError_t err = cudaGraphInstantiate(&h->exec, g, 0);
+  if (err != cudaSuccess) {
+    cudaGraphDestroy(g);
+    delete h;
+    return cuda_fail(err, "graph instantiation");
+  }
+  *out = h;
+  return SPE_OK;
+}
+
+int spe_graph_launch(spe_graph* g, void* stream) {
+  if (!g) return fail(SPE_ERR_INVALID, "null graph");
+  CK(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)), "graph launch");
+  return SPE_OK;
+}
+
+int spe_graph_destroy(spe_graph* g) {
+  if (!g) return SPE_OK;
+  cudaGraphExecDestroy(g->exec);
+  cudaGraphDestroy(g->graph);
+  delete g;
   return SPE_OK;
 }
 

@@ -43,6 +43,10 @@ struct spe_engine {
   // next, so that a block's working set stays in L2; with lanes = 2 two
   // blocks run concurrently on two streams, each kernel on half the SMs
   int chunk = 0, lanes = 1;
+  // patterns: A holds npatterns arrays of n*n; slot p uses pattern p / ipp
+  // (ipp = 0: one pattern for every slot)
+  int npatterns = 1, ipp = 0;
+  int a_cap = 1;  // patterns the A allocation holds
   cudaStream_t lane2 = nullptr;          // second lane (created on first use)
   cudaEvent_t fork = nullptr, join = nullptr, phase = nullptr;
 };
@@ -56,6 +60,11 @@ spe::Gate gate_raar(float real);
 int check_range(spe_engine* e, int first, int count);
 int need_amp(spe_engine* e);
 spe::Ctx make_ctx(spe_engine* e, int first, int count);
+// amplitudes of the pattern of slot `first`, after checking that
+// [first, first+count) lies within one pattern
+int pattern_of_range(spe_engine* e, int first, int count, const float** A);
+// context over `count` scratch items (not slots) with one pattern's amplitudes
+spe::Ctx item_ctx(spe_engine* e, int count, const float* A);
 size_t max_tiles(const spe::SizeOps* o);
 size_t region(spe_engine* e);
 int reduce(spe_engine* e, const double* part, int count, int tpi, int k, int is_max, int slot);

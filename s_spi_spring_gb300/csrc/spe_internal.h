@@ -57,6 +57,7 @@ struct Ctx {
   double* red;          // per-individual reduced values, count * 4 * slots
   int grid_div;         // persistent kernels use 1/grid_div of the resident CTAs (<= 1: all)
   cudaEvent_t mark;     // if set, recorded after the first column pass of an iteration call
+  int ipp;              // individuals per pattern (slot p uses pattern p / ipp of A); 0: A is one pattern
 };
 
 // Phase gate (see phase_out in spe_kernels.cuh): float thresholds of
@@ -105,6 +106,10 @@ struct SizeOps {
   int default_cols, default_rows;
   // partials of the column pass: sum over A >= 0 of |FFT+(rho)|^2 and A^2
   cudaError_t (*known_power)(const Ctx&, double* partials);
+  // far-field loss (0 amplitude, 1 Poisson) of items [first, first+count) of
+  // Ctx::rho / Ctx::S into column-pass partials; with grad, the adjoint
+  // gradient times scale[item] (scale may be null)
+  cudaError_t (*loss_grad)(const Ctx&, int loss, float eps, double* partials, float2* grad, const float* scale);
 };
 
 const SizeOps* size_ops(int n);

@@ -249,8 +249,14 @@ struct NoAcc {
 // ---------------------------------------------------------------------------
 struct OpBase {
   static constexpr int NSUM = 0, NMAX = 0, PEAK = 0;
-  int first;
-  double* partials;
+  int first = 0;
+  double* partials = nullptr;
+  // individuals per pattern when the engine holds several patterns (slot p
+  // uses pattern p / ipp); 0: one pattern shared by all
+  int ipp = 0;
+  __device__ __forceinline__ const float* amp(const float* A, int p, int n) const {
+    return ipp > 0 ? A + (size_t)(p / ipp) * n * n : A;
+  }
 };
 
 // Source transforms of the first row pass: rho itself, rho gated by the
@@ -297,8 +303,8 @@ struct OpColsProject : OpBase {
   using Acc = NoAcc;
   __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
   int n;
-  __device__ float2 mid(float2 v, size_t, int, int y, int x, Acc&) const {
-    return project(v, __ldg(A + (size_t)y * n + x));
+  __device__ float2 mid(float2 v, size_t, int p, int y, int x, Acc&) const {
+    return project(v, __ldg(amp(A, p, n) + (size_t)y * n + x));
   }
   __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
 };
@@ -439,8 +445,8 @@ struct OpColsError : OpBase {
     }
   };
   __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
-  __device__ float2 mid(float2 v, size_t, int, int y, int x, Acc& acc) const {
-    const float a = __ldg(A + (size_t)y * n + x);
+  __device__ float2 mid(float2 v, size_t, int p, int y, int x, Acc& acc) const {
+    const float a = __ldg(amp(A, p, n) + (size_t)y * n + x);
     const float m = cabsf2(v);
     acc.mx = fmaxf(acc.mx, m);
     if (a >= 0.f) {
@@ -548,7 +554,7 @@ struct OpColsCrossPower : OpBase {
     float2 c = make_float2(d.x * r.x - sd * r.y, d.x * r.y + sd * r.x);
     const float w = bandpass2(x, y, n, minr, maxr);
     c = make_float2(c.x * w, c.y * w);
-    if (__ldg(A + pix) < 0.f) c = make_float2(0.f, 0.f);
+    if (__ldg(amp(A, p, n) + pix) < 0.f) c = make_float2(0.f, 0.f);
     return c;
   }
   __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
@@ -599,12 +605,103 @@ struct OpColsKnownPower : OpBase {
   };
   __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
   __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
-  __device__ void store(float2 v, size_t, int, int y, int x, Acc& acc) const {
-    const float a = __ldg(A + (size_t)y * n + x);
+  __device__ void store(float2 v, size_t, int p, int y, int x, Acc& acc) const {
+    const float a = __ldg(amp(A, p, n) + (size_t)y * n + x);
     if (a >= 0.f) {
       acc.f2 += v.x * v.x + v.y * v.y;
       acc.a2 += a * a;
     }
+  }
+};
+
+// ---- far-field loss and its adjoint (gradient refinement; no reference
+// counterpart).  F = FFT+(S rho) (the transform of the iteration).  Over the
+// known pixels (A >= 0):
+//   amplitude: L = sum (|F| - A)^2,            dL/dconj(F) = (|F| - A) F/|F|
+//   Poisson:   L = sum |F|^2 - A^2 log(|F|^2 + eps), dL/dconj(F) = (1 - A^2/(|F|^2+eps)) F
+// The gradient in the convention of complex autograd (2 dL/dconj(z), the
+// steepest-ascent direction) is G = 2 S FFT-(dL/dconj(F)) (FFT- is the
+// adjoint of FFT+; no normalisation).
+enum { LOSS_AMPLITUDE = 0, LOSS_POISSON = 1 };
+
+template <int LOSS>
+__device__ __forceinline__ float loss_term(float2 F, float a, float eps, float2* g) {
+  const float m2 = F.x * F.x + F.y * F.y;
+  if (LOSS == LOSS_AMPLITUDE) {
+    const float m = sqrtf(m2);
+    const float d = m - a;
+    const float f = m > 0.f ? 2.f * d / m : 0.f;
+    if (g) *g = make_float2(f * F.x, f * F.y);
+    return d * d;
+  } else {
+    const float i = a * a;
+    const float den = m2 + eps;
+    const float f = 2.f * (1.f - i / den);
+    if (g) *g = make_float2(f * F.x, f * F.y);
+    return m2 - i * logf(den);
+  }
+}
+
+// row pass: S rho -> FFT+ (x) -> T
+struct OpRowsSupportForward : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = 0, NSUM = 0, NMAX = 0;
+  const float2* rho;
+  const int* S;
+  float2* T;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const {
+    return S[gi] > 0 ? rho[gi] : make_float2(0.f, 0.f);
+  }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int, int, int, Acc&) const { T[gi] = v; }
+};
+
+// column pass: T -> FFT+ (y) = F -> loss terms; with GRAD, -> 2 dL/dconj(F)
+// -> FFT- (y) -> T
+template <int LOSS, bool GRAD>
+struct OpColsLoss : OpBase {
+  static constexpr int FFT1 = +1, FFT2 = GRAD ? -1 : 0, NSUM = 1, NMAX = 0;
+  float2* T;
+  const float* A;
+  int n;
+  float eps;
+  struct Acc {
+    float l = 0.f;
+    __device__ void values(double (&v)[NRED]) const {
+      v[0] = l;
+      v[1] = v[2] = v[3] = 0.0;
+    }
+  };
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int p, int y, int x, Acc& acc) const {
+    const float a = __ldg(amp(A, p, n) + (size_t)y * n + x);
+    float2 g = make_float2(0.f, 0.f);
+    if (a >= 0.f) acc.l += loss_term<LOSS>(v, a, eps, &g);
+    return g;
+  }
+  __device__ void store(float2 v, size_t gi, int p, int y, int x, Acc& acc) const {
+    if (GRAD) {
+      T[gi] = v;
+    } else {
+      const float a = __ldg(amp(A, p, n) + (size_t)y * n + x);
+      if (a >= 0.f) acc.l += loss_term<LOSS>(v, a, eps, nullptr);
+    }
+  }
+};
+
+// row pass: T -> FFT- (x) -> G = scale[p] * S * (.)
+struct OpRowsGradOut : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 0, NMAX = 0;
+  const float2* T;
+  const int* S;
+  float2* G;
+  const float* scale;  // per item (upstream gradient), or null for 1
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 v, size_t, int, int, int, Acc&) const { return v; }
+  __device__ void store(float2 v, size_t gi, int p, int, int, Acc&) const {
+    const float f = S[gi] > 0 ? (scale ? scale[p - first] : 1.f) : 0.f;
+    G[gi] = make_float2(v.x * f, v.y * f);
   }
 };
 

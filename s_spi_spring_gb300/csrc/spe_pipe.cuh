@@ -80,7 +80,7 @@ __device__ __forceinline__ void load_twiddles(float2* tw, const float2* __restri
 // column pass: T -> FFT+ (y) -> P_M with A -> FFT- (y) -> T
 template <int N, int W>
 __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
-    k_cols_project(float2* __restrict__ T, const float* __restrict__ A, int first, int count,
+    k_cols_project(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count,
                    const float2* __restrict__ twg) {
   using C = ColCfg<N, W>;
   constexpr int NT = C::NT, E = C::E, TPI = N / W;
@@ -99,13 +99,14 @@ __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
     float2* sT = reinterpret_cast<float2*>(stages + s * C::STAGE);
     float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
     const float2* gT = T + (size_t)p * N * N + x0;
+    const float* Ap = ipp > 0 ? A + (size_t)(p / ipp) * N * N : A;  // the individual's pattern
     for (int q = t; q < N * W / 2; q += NT) {
       const int y = q / (W / 2), h = q - y * (W / 2);
       cp_async16(&sT[Lay::idx(y, 2 * h)], gT + (size_t)y * N + 2 * h);
     }
     for (int q = t; q < N * W / 4; q += NT) {
       const int y = q / (W / 4), h = q - y * (W / 4);
-      cp_async16(&sA[y * W + 4 * h], A + (size_t)y * N + x0 + 4 * h);
+      cp_async16(&sA[y * W + 4 * h], Ap + (size_t)y * N + x0 + 4 * h);
     }
   };
 
@@ -315,7 +316,7 @@ __device__ __forceinline__ void fft_pair(float2* a, float2* b, float4* buf, cons
 // column pass, two columns per thread: T -> FFT+ (y) -> P_M -> FFT- (y) -> T
 template <int N, int WP>
 __global__ void __launch_bounds__(PairCfg<N, WP>::NT, PairCfg<N, WP>::MINB)
-    k_cols_pair(float2* __restrict__ T, const float* __restrict__ A, int first, int count,
+    k_cols_pair(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count,
                 const float2* __restrict__ twg) {
   using C = PairCfg<N, WP>;
   constexpr int NT = C::NT, E = C::E, W = C::W, TPI = N / W;
@@ -335,13 +336,14 @@ __global__ void __launch_bounds__(PairCfg<N, WP>::NT, PairCfg<N, WP>::MINB)
     float4* sT = reinterpret_cast<float4*>(stages + s * C::STAGE);
     float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
     const float2* gT = T + (size_t)p * N * N + x0;
+    const float* Ap = ipp > 0 ? A + (size_t)(p / ipp) * N * N : A;  // the individual's pattern
     for (int q = t; q < N * WP; q += NT) {
       const int y = q / WP, hh = q - y * WP;
       cp_async16(&sT[Lay::idx(y, hh)], gT + (size_t)y * N + 2 * hh);
     }
     for (int q = t; q < N * W / 4; q += NT) {
       const int y = q / (W / 4), hh = q - y * (W / 4);
-      cp_async16(&sA[y * W + 4 * hh], A + (size_t)y * N + x0 + 4 * hh);
+      cp_async16(&sA[y * W + 4 * hh], Ap + (size_t)y * N + x0 + 4 * hh);
     }
   };
 

@@ -398,7 +398,7 @@ int average_module_dev(spe_engine* e, int first, int count, const std::vector<in
   const size_t npix = e->npix;
   float* M = cv.take<float>((size_t)count * npix);
   int* ord = cv.take<int>(count);
-  spe::Ctx c = make_ctx(e, 0, count);
+  spe::Ctx c = item_ctx(e, count, e->A);  // (transforms only; no amplitudes read)
   if (ft) {
     float2* tmp = cv.take<float2>((size_t)count * npix);
     CK(e->ops->ft_magnitude(c, e->rho + (size_t)first * npix, tmp, M), "average module transforms");
@@ -431,6 +431,8 @@ int spe_reshift(spe_engine* e, int first, int count, int ref_slot, const float* 
   if (ref_slot < 0 && !ref_density) return fail(SPE_ERR_INVALID, "no reference density");
   if (ref_slot >= e->cap) return fail(SPE_ERR_INVALID, "reference slot %d outside capacity %d", ref_slot, e->cap);
   if (count == 0) return SPE_OK;
+  const float* Apat = nullptr;
+  if ((rc = pattern_of_range(e, first, count, &Apat))) return rc;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   const size_t npix = e->npix;
   const int tr = e->ops->tiles_rows;
@@ -455,9 +457,9 @@ int spe_reshift(spe_engine* e, int first, int count, int ref_slot, const float* 
        "reference copy");
   else
     CK(cudaMemcpyAsync(e->ref, ref_density, npix * sizeof(float2), cudaMemcpyHostToDevice, e->st), "reference upload");
-  spe::Ctx c = make_ctx(e, 0, count);
+  spe::Ctx c = item_ctx(e, count, Apat);
   CK(e->ops->abs_spectrum_items(c, e->rho + (size_t)first * npix, D), "spectra");
-  spe::Ctx c1 = make_ctx(e, 0, 1);
+  spe::Ctx c1 = item_ctx(e, 1, Apat);
   CK(e->ops->abs_spectrum_items(c1, e->ref, D + (size_t)count * npix), "reference spectrum");
   spe::k_complex_sum<<<count, 256, 0, e->st>>>(e->rho + (size_t)first * npix, npix, nullptr, sums);
   spe::k_complex_sum<<<1, 256, 0, e->st>>>(e->ref, npix, nullptr, sums + 2 * count);
@@ -651,6 +653,8 @@ int spe_crossover(spe_engine* e, int first, int count, const float* errors, int 
   for (int s : {best_slot, avg_slot})
     if (s < 0 || s >= e->cap || (s >= dst_first && s < dst_first + count))
       return fail(SPE_ERR_INVALID, "best/average slot %d invalid", s);
+  const float* Apat = nullptr;
+  if ((rc = pattern_of_range(e, first, count, &Apat))) return rc;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   const int n = e->n;
   const size_t npix = e->npix;
@@ -745,9 +749,9 @@ int spe_crossover(spe_engine* e, int first, int count, const float* errors, int 
     // ---- alignment of self, p2, p3 and the average to p1
     // (prepare_parents / reshift_parent, gpu_context.cu:1536-1694; spectra
     // not normalised on this path).  Spectra of the members and the average.
-    spe::Ctx c = make_ctx(e, 0, P);
+    spe::Ctx c = item_ctx(e, P, Apat);
     CK(e->ops->abs_spectrum_items(c, e->rho + (size_t)first * npix, D), "spectra");
-    CK(e->ops->abs_spectrum_items(make_ctx(e, 0, 1), e->rho + (size_t)avg_slot * npix, D + (size_t)P * npix),
+    CK(e->ops->abs_spectrum_items(item_ctx(e, 1, Apat), e->rho + (size_t)avg_slot * npix, D + (size_t)P * npix),
        "average spectrum");
     spe::k_complex_sum<<<P, 256, 0, e->st>>>(e->rho + (size_t)first * npix, npix, nullptr, sums);
     spe::k_complex_sum<<<1, 256, 0, e->st>>>(e->rho + (size_t)avg_slot * npix, npix, nullptr, sums + 2 * P);
@@ -762,7 +766,7 @@ int spe_crossover(spe_engine* e, int first, int count, const float* errors, int 
     }
     CK(cudaMemcpyAsync(xi, hx.data(), items * sizeof(int), cudaMemcpyHostToDevice, e->st), "pairs");
     CK(cudaMemcpyAsync(ri, hr.data(), items * sizeof(int), cudaMemcpyHostToDevice, e->st), "pairs");
-    spe::Ctx ci = make_ctx(e, 0, items);
+    spe::Ctx ci = item_ctx(e, items, Apat);
     for (int s = 0; s < 2; ++s) {
       CK(e->ops->corr_peak_idx(ci, D, D, xi, ri, s == 0 ? -1 : +1, minr, maxr, 0, 0, scratch, part), "correlation");
       spe::k_reduce_peak<<<(items + 127) / 128, 128, 0, e->st>>>(part, items, tr, peaks, 4, 2 * s);
@@ -815,16 +819,16 @@ int spe_crossover(spe_engine* e, int first, int count, const float* errors, int 
     CK(cudaGetLastError(), "parent gather");
 
     // ---- Fourier-space children: transform their five parents
-    if (ncft > 0) CK(e->ops->fft2(make_ctx(e, 0, 5 * ncft), W, +1), "parent transforms");
+    if (ncft > 0) CK(e->ops->fft2(item_ctx(e, 5 * ncft, Apat), W, +1), "parent transforms");
     CK(cudaMemcpyAsync(dch, ch.data(), P * sizeof(spe::CrossChild), cudaMemcpyHostToDevice, e->st), "children");
     CK(cudaMemcpyAsync(dcm, cmaps.data(), cmaps.size() * sizeof(int), cudaMemcpyHostToDevice, e->st), "crossmaps");
     dim3 gridc((unsigned)((npix + 255) / 256), (unsigned)P);
-    spe::k_cross<<<gridc, 256, 0, e->st>>>(W, C, dch, dcm, (int)cmaps.size(), e->A, e->avg_mod, n, crossdiff,
+    spe::k_cross<<<gridc, 256, 0, e->st>>>(W, C, dch, dcm, (int)cmaps.size(), Apat, e->avg_mod, n, crossdiff,
                                            use_average, crosssym);
     CK(cudaGetLastError(), "crossover");
     spe::k_cross_support<<<gridc, 256, 0, e->st>>>(Ws, e->S, dch, npix);
     CK(cudaGetLastError(), "crossover support");
-    if (ncft > 0) CK(e->ops->fft2(make_ctx(e, 0, ncft), C, -1), "child transforms");
+    if (ncft > 0) CK(e->ops->fft2(item_ctx(e, ncft, Apat), C, -1), "child transforms");
     std::vector<int> hself(P), hdst(P);
     for (int i = 0; i < P; ++i) {
       hself[i] = first + i;

@@ -120,7 +120,7 @@ cudaError_t launch_cols_project(const Ctx& c) {
   const int tiles = c.count * (N / W);
   const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
-  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
+  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.ipp, c.first, c.count, c.tw);
   return cudaGetLastError();
 }
 
@@ -150,7 +150,7 @@ cudaError_t launch_cols_pair(const Ctx& c) {
   const int tiles = c.count * (N / W);
   const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
-  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.first, c.count, c.tw);
+  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.ipp, c.first, c.count, c.tw);
   return cudaGetLastError();
 }
 
@@ -212,6 +212,7 @@ struct SizeImpl {
     op.T = c.T;
     op.A = c.A;
     op.n = N;
+    op.ipp = c.ipp;
     return op;
   }
 
@@ -308,6 +309,7 @@ struct SizeImpl {
     ce.T = c.T;
     ce.A = c.A;
     ce.n = N;
+    ce.ipp = c.ipp;
     SPE_TRY((launch_pass<N, AX_COLS>(ce, c.count, c.st, c.tw)));
     OpRowsRealError re;
     re.first = c.first;
@@ -343,6 +345,7 @@ struct SizeImpl {
     cp.dst = c.T;
     cp.A = c.A;
     cp.n = N;
+    cp.ipp = c.ipp;
     cp.minr = minr;
     cp.maxr = maxr;
     cp.norm_d = norm_d;
@@ -461,7 +464,55 @@ struct SizeImpl {
     kp.T = c.T;
     kp.A = c.A;
     kp.n = N;
+    kp.ipp = c.ipp;
     return launch_pass<N, AX_COLS>(kp, c.count, c.st, c.tw);
+  }
+
+  // far-field loss per item into partials (column-pass tiles); with grad,
+  // grad = scale[p] * 2 S FFT-(dL/dconj F) for items [first, first+count)
+  // of c.rho / c.S (c.T is scratch)
+  template <int LOSS>
+  static cudaError_t loss_grad_t(const Ctx& c, float eps, double* partials, float2* grad, const float* scale) {
+    OpRowsSupportForward rf;
+    rf.first = c.first;
+    rf.partials = nullptr;
+    rf.rho = c.rho;
+    rf.S = c.S;
+    rf.T = c.T;
+    SPE_TRY((launch_pass<N, AX_ROWS>(rf, c.count, c.st, c.tw)));
+    if (!grad) {
+      OpColsLoss<LOSS, false> cl;
+      cl.first = c.first;
+      cl.partials = partials;
+      cl.T = c.T;
+      cl.A = c.A;
+      cl.n = N;
+      cl.ipp = c.ipp;
+      cl.eps = eps;
+      return launch_pass<N, AX_COLS>(cl, c.count, c.st, c.tw);
+    }
+    OpColsLoss<LOSS, true> cg;
+    cg.first = c.first;
+    cg.partials = partials;
+    cg.T = c.T;
+    cg.A = c.A;
+    cg.n = N;
+    cg.ipp = c.ipp;
+    cg.eps = eps;
+    SPE_TRY((launch_pass<N, AX_COLS>(cg, c.count, c.st, c.tw)));
+    OpRowsGradOut go;
+    go.first = c.first;
+    go.partials = nullptr;
+    go.T = c.T;
+    go.S = c.S;
+    go.G = grad;
+    go.scale = scale;
+    return launch_pass<N, AX_ROWS>(go, c.count, c.st, c.tw);
+  }
+  static cudaError_t loss_grad(const Ctx& c, int loss, float eps, double* partials, float2* grad,
+                               const float* scale) {
+    return loss == LOSS_POISSON ? loss_grad_t<LOSS_POISSON>(c, eps, partials, grad, scale)
+                                : loss_grad_t<LOSS_AMPLITUDE>(c, eps, partials, grad, scale);
   }
 
   static const SizeOps* table() {
@@ -483,7 +534,8 @@ struct SizeImpl {
                               &SizeImpl<N>::row_widths,
                               DefaultTiles<N>::cols,
                               DefaultTiles<N>::rows,
-                              &SizeImpl<N>::known_power};
+                              &SizeImpl<N>::known_power,
+                              &SizeImpl<N>::loss_grad};
     return &t;
   }
 };
