@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
+    ap.add_argument("--batch-patterns", type=int, default=256,
+                    help="patterns of uneven sizes in the graph-captured batch (0: skip)")
     ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
     ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
@@ -260,6 +262,55 @@ def memetic(args, local, tiles, sched):
                     "ops of both sequences"}
 
 
+def batched_sizes(args, local):
+    """Uneven sizes in one graph: patterns with sides drawn from
+    {256, 384, 512, 768, 1024}, photons log-uniform in 1e5..1e8, beamstop
+    radius 4..12 px and 0..3 gap stripes, population 16 each; one sweep =
+    HIO (20 iterations, beta 0.9) then ER (10) on every individual, replayed
+    from one CUDA graph.  Rates count pixel-iterations and
+    individual-iterations over all patterns."""
+    import torch
+    from s_spi_spring_gb300 import synthetic
+    from s_spi_spring_gb300.batch import PatternBatch
+    rng = np.random.default_rng(2)
+    sides = rng.choice([256, 384, 512, 768, 1024], size=args.batch_patterns)
+    pats = []
+    for k, n in enumerate(sides):
+        I, _, _ = synthetic.polygon_pattern(seed=1000 + k, n=int(n), diameter=float(n) * 0.23,
+                                            photons=float(10 ** rng.uniform(5, 8)),
+                                            stop_radius=float(rng.uniform(4, 12)), gap=4,
+                                            stripes=int(rng.integers(0, 4)))
+        pats.append(I)
+    b = PatternBatch(pats, population=16, device=local)
+    b.initialize()
+    tuned = b.autotune(iterations=2)
+    hio, er = 20, 10
+    b.capture(hio, 0.9, er)
+    stream = torch.cuda.ExternalStream(b.stream, device=f"cuda:{local}")
+    for _ in range(max(1, args.warmup)):
+        b.run()
+    b.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.run()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    m = b.evaluate()
+    rf = [x["error_fourier"] for v in m.values() for x in v]
+    out = {"patterns": int(args.batch_patterns),
+           "sides": {int(n): int(len(g["ids"])) for n, g in b.sizes.items()},
+           "individuals": b.individuals(), "iterations_per_sweep": hio + er, "ms_per_sweep": round(ms, 3),
+           "px_iter_per_s": round(b.pixels_per_iteration() * (hio + er) / (ms / 1e3), 1),
+           "iter_ind_per_s": round(b.individuals() * (hio + er) / (ms / 1e3), 1),
+           "graph": "one CUDA graph launch per sweep (all sizes)",
+           "tuned": {int(n): v for n, v in tuned.items()},
+           "rfactor_median": round(float(np.median(rf)), 5)}
+    b.close()
+    return out
+
+
 def run_engine(args):
     import torch
     from s_spi_spring_gb300 import _lib
@@ -388,6 +439,11 @@ def run_engine(args):
             out["plain_gpu"]["fused_over_plain"] = round(value / world / out["plain_gpu"]["value"], 3)
         except Exception as ex:
             out["plain_gpu"] = {"error": str(ex)[:200]}
+    if rank == 0 and args.batch_patterns > 0:
+        try:
+            out["batched_sizes"] = batched_sizes(args, local)
+        except Exception as ex:
+            out["batched_sizes"] = {"error": str(ex)[:300]}
     if rank == 0 and args.memetic_gens > 0:
         try:
             out["memetic"] = memetic(args, local, tiles, sched)

@@ -165,6 +165,14 @@ int spe_sequence(spe_engine* e, int first, int count, const spe_op* ops, int nop
  * (0+1)*seed (src/solver.cpp:37, src/context.h:13). */
 int spe_seed(spe_engine* e, uint32_t seed);
 
+/* The generator's full state as text (the C++ standard library's stream
+ * form of std::mt19937), for checkpoints: a run resumed with
+ * spe_set_rng_state draws exactly what the uninterrupted run would have (no
+ * reference counterpart: the reference cannot resume).  buf may be NULL to
+ * query the length (including the terminating zero). */
+int spe_get_rng_state(spe_engine* e, char* buf, int capacity, int* length);
+int spe_set_rng_state(spe_engine* e, const char* state);
+
 /* Solver::Reshift (src/solver.cpp:511-538) with GPU_context::set_ref_density,
  * get_shift and reshift (gpu_context.cu:632-667, 1226-1371): aligns each
  * individual of [first, first+count) to the reference (translation, global
@@ -268,6 +276,11 @@ int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, in
  * are configured on their first launch.  spe_graph_launch replays the whole
  * recording as one graph launch on any stream. */
 typedef struct spe_graph spe_graph;
+/* A non-blocking stream on the current device, for engines that share one
+ * (capture, ordering across engines).  A stream given to spe_set_stream
+ * must outlive the engines that use it. */
+int spe_stream_create(void** stream);
+int spe_stream_destroy(void* stream);
 int spe_graph_begin(void* stream);
 int spe_graph_end(void* stream, spe_graph** out);
 int spe_graph_launch(spe_graph* g, void* stream);

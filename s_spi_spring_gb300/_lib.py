@@ -79,11 +79,26 @@ SIGNATURES = {
     "spe_gather": (_i, [_vp, _ip, _i, _i]),
     "spe_loss_grad": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp, _vp]),
     "spe_set_amplitudes_batch": (_i, [_vp, _fp, _i, _i]),
+    "spe_get_rng_state": (_i, [_vp, C.c_char_p, _i, C.POINTER(_i)]),
+    "spe_set_rng_state": (_i, [_vp, C.c_char_p]),
+    "spe_stream_create": (_i, [C.POINTER(_vp)]),
+    "spe_stream_destroy": (_i, [_vp]),
     "spe_graph_begin": (_i, [_vp]),
     "spe_graph_end": (_i, [_vp, C.POINTER(_vp)]),
     "spe_graph_launch": (_i, [_vp, _vp]),
     "spe_graph_destroy": (_i, [_vp]),
 }
+
+
+def stream_create() -> int:
+    """A non-blocking CUDA stream (handle) on the current device."""
+    st = _vp()
+    call("spe_stream_create", C.byref(st))
+    return st.value
+
+
+def stream_destroy(handle: int):
+    call("spe_stream_destroy", _vp(handle))
 
 
 class Graph:
@@ -247,6 +262,11 @@ class Engine:
     def set_stream(self, stream_handle: int | None):
         call("spe_set_stream", self.h, _vp(stream_handle or 0))
 
+    def get_stream(self) -> int:
+        st = _vp()
+        call("spe_get_stream", self.h, C.byref(st))
+        return st.value or 0
+
     def device_buffers(self):
         d, s = _vp(), _vp()
         call("spe_device_buffers", self.h, C.byref(d), C.byref(s))
@@ -306,6 +326,16 @@ class Engine:
         return a.value, b.value
 
     # -- population-level operations --------------------------------------------
+    def rng_state(self) -> str:
+        n = C.c_int()
+        call("spe_get_rng_state", self.h, None, 0, C.byref(n))
+        buf = C.create_string_buffer(n.value)
+        call("spe_get_rng_state", self.h, buf, n.value, C.byref(n))
+        return buf.value.decode()
+
+    def set_rng_state(self, state: str):
+        call("spe_set_rng_state", self.h, state.encode())
+
     def seed(self, seed: int):
         call("spe_seed", self.h, C.c_uint32(int(seed) & 0xFFFFFFFF))
 

@@ -760,6 +760,21 @@ struct spe_graph {
   cudaGraphExec_t exec = nullptr;
 };
 
+int spe_stream_create(void** out) {
+  if (!out) return fail(SPE_ERR_INVALID, "null argument");
+  cudaStream_t s = nullptr;
+  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+  *out = s;
+  return SPE_OK;
+}
+
+int spe_stream_destroy(void* stream) {
+  if (!stream) return SPE_OK;
+  CK(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "stream synchronize");
+  CK(cudaStreamDestroy(static_cast<cudaStream_t>(stream)), "stream destroy");
+  return SPE_OK;
+}
+
 int spe_graph_begin(void* stream) {
   if (!stream) return fail(SPE_ERR_INVALID, "capture needs an explicit stream");
   CK(cudaStreamBeginCapture(static_cast<cudaStream_t>(stream), cudaStreamCaptureModeThreadLocal), "begin capture");

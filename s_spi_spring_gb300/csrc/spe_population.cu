@@ -10,6 +10,8 @@
 #include <cstring>
 #include <numeric>
 #include <random>
+#include <sstream>
+#include <string>
 #include <vector>
 
 #include "../../include/spe_engine.h"
@@ -421,6 +423,28 @@ extern "C" {
 int spe_seed(spe_engine* e, uint32_t seed) {
   if (!e) return fail(SPE_ERR_INVALID, "null engine");
   e->rng.seed(seed);
+  return SPE_OK;
+}
+
+int spe_get_rng_state(spe_engine* e, char* buf, int capacity, int* length) {
+  if (!e || !length) return fail(SPE_ERR_INVALID, "null argument");
+  std::ostringstream os;
+  os << e->rng;
+  const std::string st = os.str();
+  *length = (int)st.size() + 1;
+  if (!buf) return SPE_OK;
+  if (capacity < *length) return fail(SPE_ERR_INVALID, "state needs %d bytes, buffer holds %d", *length, capacity);
+  std::memcpy(buf, st.c_str(), st.size() + 1);
+  return SPE_OK;
+}
+
+int spe_set_rng_state(spe_engine* e, const char* state) {
+  if (!e || !state) return fail(SPE_ERR_INVALID, "null argument");
+  std::istringstream is(state);
+  std::mt19937 r;
+  is >> r;
+  if (is.fail()) return fail(SPE_ERR_INVALID, "not a generator state");
+  e->rng = r;
   return SPE_OK;
 }
 

@@ -170,6 +170,44 @@ class MemeticSettings:
                                  int(np.round(self.decay_end * self.generations)))
 
 
+class Stats:
+    """Per-generation statistics of the population (``spring/stats_manager.py``
+    ``Stats.add``): best, average-reconstruction and mean values of error,
+    complexity (reality), symmetry, module and complex sums, plus the
+    oversampling of the best support, the generation, the replaced fraction
+    and a time stamp."""
+
+    ENTRIES = ("error", "complexity", "symmetry", "module_sum", "complex_sum")
+
+    def __init__(self):
+        self.stats = {k: {e: [] for e in self.ENTRIES} for k in ("best", "average", "mean", "all")}
+        self.stats["global"] = {"OS": [], "generation": [], "replacement": [], "tstamp": []}
+
+    @staticmethod
+    def _values(r):
+        return (r.get_error(), r.get_reality(), r.get_symmetry(), r.get_module_sum(), r.get_complex_sum())
+
+    def add(self, recs, best, avg, replcount, generation, tstamp, best_support_pixels):
+        vals = np.array([self._values(r) for r in recs], dtype=np.float64)
+        b = int(np.argmin(vals[:, 0]))
+        for i, e in enumerate(self.ENTRIES):
+            self.stats["best"][e].append(vals[b, i])
+            self.stats["average"][e].append(self._values(avg)[i])
+            self.stats["mean"][e].append(float(np.mean(vals[:, i])))
+            self.stats["all"][e].append(vals[:, i].tolist())
+        n = best.dims[0] * best.dims[1]
+        self.stats["global"]["OS"].append(n / best_support_pixels if best_support_pixels else float("inf"))
+        self.stats["global"]["generation"].append(generation)
+        self.stats["global"]["replacement"].append(replcount / len(recs))
+        self.stats["global"]["tstamp"].append(tstamp)
+
+    def get(self):
+        return self.stats
+
+    def set(self, stats):
+        self.stats = stats
+
+
 class MemeticRun:
     """``MPR.run`` without the result files and the hypervisor: the
     population goes through `generations` rounds of shrink-wrap, alignment,
@@ -183,6 +221,7 @@ class MemeticRun:
         self.generation = 0
         self.replcount = 0
         self.history = []  # per generation: best error, mean error, replacements, seconds
+        self.stats = Stats()
         self.solver.set_shift_param(shiftmin=settings.shift_min, shiftmax=settings.shift_max)
 
     # mpr.py:421-447
@@ -248,9 +287,12 @@ class MemeticRun:
         self._record(time.perf_counter() - t0)
 
     def _record(self, seconds):
+        """``MPR.save_result``'s statistics (``mpr.py:385-390``)."""
         errs = np.array([r.get_error() for r in self.recs])
         self.history.append({"generation": self.generation, "best": float(errs.min()), "mean": float(errs.mean()),
                              "replaced": self.replcount, "seconds": seconds})
+        self.stats.add(self.recs, self.best, self.avg, self.replcount, self.generation, time.time(),
+                       int(np.sum(self.best.get_support())))
 
     def run(self, generations=None):
         if self.generation == 0 and not self.history:

@@ -266,6 +266,8 @@ class Solver:
         self.seed = int(seed)
         gpus = list(np.atleast_1d(gpus)) if gpus is not None else []
         self.device = int(gpus[0]) if len(gpus) else 0
+        self.use_bounds = bool(use_bounds)
+        self.intensities = pat.copy()  # the input pattern (kept for result files and resume)
         self.pattern = _lib.prepare_pattern(pat, self.center, use_bounds)
         self.engine = _lib.Engine(self.dims[0], self.device)
         self.engine.set_amplitudes(self.pattern)

@@ -33,7 +33,10 @@ def _intensity(obj: np.ndarray, photons: float, rng) -> np.ndarray:
     n = obj.shape[0]
     F = np.fft.ifft2(obj) * (n * n)
     I = np.abs(np.fft.fftshift(F)) ** 2
-    I *= photons / I.sum()
+    total = I.sum()
+    if not total > 0:
+        raise ValueError("empty object: no scattered intensity")
+    I *= photons / total
     return rng.poisson(I).astype(np.float32)
 
 
@@ -68,10 +71,13 @@ def _convex_polygon(rng, n, diameter, nv):
 
 def polygon_pattern(seed: int = 1, n: int = 512, diameter: float = 120.0, photons: float = 1e7,
                     stop_radius: float = 8.0, gap: int = 4, stripes: int = 2):
-    """Returns (intensities, true_object, true_support)."""
+    """Seeded convex polygon (6-12 vertices, `diameter` pixels across),
+    density uniform in [0.3, 1], phase noise 0.2 rad; Poisson intensities
+    with `photons` in total; a masked central disc and `stripes` gap stripes
+    of `gap` pixels.  Returns (intensities, true_object, true_support)."""
     rng = np.random.default_rng(seed)
     nv = int(rng.integers(6, 13))
-    supp = _convex_polygon(rng, n, diameter * n / 512.0 if n < 512 else diameter, nv)
+    supp = _convex_polygon(rng, n, diameter, nv)
     dens = rng.uniform(0.3, 1.0, (n, n))
     ph = rng.normal(0.0, 0.2, (n, n))
     obj = np.where(supp, dens * np.exp(1j * ph), 0).astype(np.complex128)

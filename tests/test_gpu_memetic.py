@@ -68,3 +68,33 @@ def test_resident_loop_equals_host_round_trips():
 def test_hio_loop_with_stabilisation_and_sw_first():
     r = run(alg="HIO", beta=0.9, it_stab=3, sw_first=True, generations=2, repetitions=4)
     assert np.isfinite(r.history[-1]["best"])
+
+
+def test_checkpoint_resume_is_bit_identical(tmp_path):
+    """Four generations straight versus two, a checkpoint, a fresh solver
+    resumed from it, and two more: same populations and statistics."""
+    from s_spi_spring_gb300.checkpoint import load_checkpoint, resume, save_checkpoint
+    straight = run(generations=4)
+    # the same set-up stopped after two generations, checkpointed, resumed
+    # in a new solver
+    s = settings(generations=4)
+    I, _, _ = synthetic.polygon_pattern(seed=11, n=128, diameter=128 * 0.25, photons=1e8, stop_radius=3)
+    sol = Solver(I, gpus=[0], seed=42, use_bounds=False)
+    recs = sol.InitializePop(s.popsize, int(128 * 0.35), itemsize=[128 * 0.35 * 0.2, 128 * 0.35 * 0.9],
+                             nitems=[2, 8], exponent=[0.5, 0.5], scaling=[0.5, 1.5], phaserange=0)
+    part = MemeticRun(sol, recs, s).run(generations=2)
+    path = tmp_path / "ckpt.npz"
+    save_checkpoint(path, part)
+    c = load_checkpoint(path)
+    for key in ("pid", "settings", "pattern", "density_best", "support_best", "density_avg", "support_avg",
+                "density_all", "support_all", "stats/best/error", "stats/global/OS", "process/generation",
+                "process/totgenerations", "process/proc_id"):
+        assert key in c, key
+    assert int(c["process/generation"]) == 2
+    del part, sol, recs
+    resumed = resume(path).run()
+    assert resumed.generation == 4
+    assert [h["best"] for h in resumed.history] == [h["best"] for h in straight.history]
+    for ra, rb in zip(straight.recs, resumed.recs):
+        assert np.array_equal(ra.get_density().view(np.uint32), rb.get_density().view(np.uint32))
+    assert resumed.stats.get()["best"]["error"] == straight.stats.get()["best"]["error"]

@@ -150,7 +150,10 @@ def test_converged_rfactor_matches_oracle(alg, beta):
     """200 iterations then 50 ER with the true support: the final R-factor
     agrees with the float64 oracle within 1e-4."""
     n = 128
-    I, obj, supp = synthetic.polygon_pattern(seed=31, n=n, diameter=40, photons=1e9, stop_radius=2)
+    # a small object (10 px across, oversampling ~160): from a random start
+    # both the float32 kernels and the float64 oracle converge to the same
+    # fixed point, so their final R-factors are comparable
+    I, obj, supp = synthetic.polygon_pattern(seed=31, n=n, diameter=10, photons=1e9, stop_radius=2)
     A = _lib.prepare_pattern(I, (-1, -1), True)
     dens, _ = synthetic.start_population(n, 2, 22, seed=32)
     S = np.broadcast_to(supp, (2, n, n)).copy()
