@@ -269,7 +269,16 @@ void fill_twiddles(float2* out) {
 // v[u*R + r] = element at position (j + TPT*u) + r*L/R of the first pass on
 // entry, of the last pass on exit (same positions: first radix == last).
 // ---------------------------------------------------------------------------
-template <int L, int TPT, int S, class Lay, int P, int NS>
+// barrier between the exchange stores and loads: the whole CTA, or (when
+// every sequence lives inside one warp) the warp
+struct SyncCTA {
+  static __device__ __forceinline__ void sync() { __syncthreads(); }
+};
+struct SyncWarp {
+  static __device__ __forceinline__ void sync() { __syncwarp(); }
+};
+
+template <int L, int TPT, int S, class Lay, int P, int NS, class Sync = SyncCTA>
 __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf, const float2* __restrict__ tw,
                                              int c, int j) {
   using Rad = typename Plan<L>::R;
@@ -302,7 +311,7 @@ __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf
 #pragma unroll
       for (int q = 0; q < R; ++q) buf[Lay::idx(base + q * NS, c)] = v[u * R + q];
     }
-    __syncthreads();
+    Sync::sync();
     constexpr int R2 = Rad::value[P + 1];
     constexpr int NB2 = L / R2;
     constexpr int U2 = NB2 / TPT;
@@ -313,8 +322,8 @@ __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf
 #pragma unroll
       for (int r = 0; r < R2; ++r) v[u * R2 + r] = buf[Lay::idx(b + r * NB2, c)];
     }
-    __syncthreads();
-    fft_pass_reg<L, TPT, S, Lay, P + 1, NS * R>(v, buf, tw, c, j);
+    Sync::sync();
+    fft_pass_reg<L, TPT, S, Lay, P + 1, NS * R, Sync>(v, buf, tw, c, j);
   }
 }
 
@@ -329,6 +338,16 @@ template <int L>
 struct Elems {
   static constexpr int value = L / Plan<L>::TPT;
 };
+
+// Position of element e of thread j of TPT (first-pass inputs / last-pass
+// outputs).
+template <int L, int TPT>
+__device__ __forceinline__ int elem_pos_t(int e, int j) {
+  constexpr int R = Plan<L>::R::value[0];
+  constexpr int NB = L / R;
+  const int u = e / R, r = e - u * R;
+  return (j + TPT * u) + r * NB;
+}
 
 // Position of element e of thread j (first-pass inputs / last-pass outputs).
 template <int L>

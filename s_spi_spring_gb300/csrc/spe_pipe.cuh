@@ -18,6 +18,14 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
@@ -384,6 +392,103 @@ __global__ void __launch_bounds__(PairCfg<N, WP>::NT, PairCfg<N, WP>::MINB)
 #pragma unroll
     for (int e = 0; e < E; ++e)
       *reinterpret_cast<float4*>(gT + (size_t)elem_pos<N>(e, j) * N) = make_float4(a[e].x, a[e].y, b[e].x, b[e].y);
+    __syncthreads();  // stage s is refilled by the next iteration's prefetch
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Column pass with one warp per column: E = N/32 elements per thread, so the
+// exchanges between radix passes are warp-synchronous and the CTA meets at
+// barriers only three times per tile (stage ready, results in shared memory,
+// stage released).  The stage holds the tile column-major (each column
+// padded like a row of the row pass); results go back to HBM as row
+// segments of 16-byte column pairs through the same buffer.
+// ---------------------------------------------------------------------------
+template <int L, int W>
+struct LayColMajor {
+  static constexpr int CS0 = L + L / 16;
+  // column stride = 2 (mod 16) elements: the 16 lanes of a half-warp that
+  // stage or drain two rows of 8 columns hit 16 different bank pairs
+  static constexpr int CS = CS0 + (18 - CS0 % 16) % 16;
+  static constexpr int SIZE = W * CS;
+  static __device__ __forceinline__ int idx(int l, int c) { return c * CS + l + (l >> 4); }
+};
+
+template <int N, int W>
+struct WarpCfg {
+  static constexpr int TPT = 32;
+  static constexpr int E = N / TPT;
+  static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
+  static constexpr int NT = W * TPT;
+  static constexpr int ACS = N + (36 - N % 32) % 32;  // amplitude column stride = 4 (mod 32) words
+  static constexpr int C_T = align128(LayColMajor<N, W>::SIZE * 8);
+  static constexpr int C_A = align128(W * ACS * 4);
+  static constexpr int STAGE = C_T + C_A;
+  static constexpr size_t SMEM = (size_t)TWB + 2 * STAGE;
+  static constexpr int MINB_RAW = 65536 / (NT * 128);
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
+};
+
+template <int N, int W>
+__global__ void __launch_bounds__(WarpCfg<N, W>::NT, WarpCfg<N, W>::MINB)
+    k_cols_warp(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count,
+                const float2* __restrict__ twg) {
+  using C = WarpCfg<N, W>;
+  constexpr int NT = C::NT, E = C::E, TPI = N / W, ACS = C::ACS;
+  using Lay = LayColMajor<N, W>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  float2* tw = reinterpret_cast<float2*>(sm);
+  unsigned char* stages = sm + C::TWB;
+  load_twiddles<N>(tw, twg, NT);
+  const int t = threadIdx.x;
+  const int c = t >> 5, j = t & 31;
+  const int ntiles = count * TPI;
+
+  auto stage_tile = [&](int tile, int s) {
+    const int p = first + tile / TPI;
+    const int x0 = (tile % TPI) * W;
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::STAGE);
+    float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
+    const float2* gT = T + (size_t)p * N * N + x0;
+    const float* Ap = (ipp > 0 ? A + (size_t)(p / ipp) * N * N : A) + x0;
+    for (int q = t; q < N * W; q += NT) {
+      const int y = q / W, cc = q - y * W;
+      cp_async8(&sT[Lay::idx(y, cc)], gT + (size_t)y * N + cc);
+      cp_async4(&sA[cc * ACS + y], Ap + (size_t)y * N + cc);
+    }
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) stage_tile(tile, 0);
+  cp_async_commit();
+  for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) stage_tile(nxt, (k + 1) & 1);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    const int s = k & 1;
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::STAGE);
+    const float* sA = reinterpret_cast<const float*>(stages + s * C::STAGE + C::C_T);
+    const int p = first + tile / TPI;
+    const int x0 = (tile % TPI) * W;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = sT[Lay::idx(elem_pos_t<N, 32>(e, j), c)];
+    __syncwarp();  // column c's region becomes this warp's exchange buffer
+    fft_pass_reg<N, 32, +1, Lay, 0, 1, SyncWarp>(v, sT, tw, c, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = project(v[e], sA[c * ACS + elem_pos_t<N, 32>(e, j)]);
+    fft_pass_reg<N, 32, -1, Lay, 0, 1, SyncWarp>(v, sT, tw, c, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) sT[Lay::idx(elem_pos_t<N, 32>(e, j), c)] = v[e];
+    __syncthreads();  // every column of the tile is in shared memory
+    float2* gT = T + (size_t)p * N * N + x0;
+    for (int q = t; q < N * W / 2; q += NT) {
+      const int y = q / (W / 2), h = q - y * (W / 2);
+      const float2 a = sT[Lay::idx(y, 2 * h)], b = sT[Lay::idx(y, 2 * h + 1)];
+      *reinterpret_cast<float4*>(gT + (size_t)y * N + 2 * h) = make_float4(a.x, a.y, b.x, b.y);
+    }
     __syncthreads();  // stage s is refilled by the next iteration's prefetch
   }
 }

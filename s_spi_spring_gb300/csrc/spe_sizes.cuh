@@ -77,6 +77,20 @@ constexpr bool pair_ok() {
   return W % 4 == 0 && W <= N && N % W == 0 && Elems<N>::value <= 8 && PairCfg<N, W / 2>::NT % 32 == 0 &&
          PairCfg<N, W / 2>::NT <= 1024 && PairCfg<N, W / 2>::SMEM <= kMaxSmem;
 }
+// one-warp-per-column variants: every pass's butterflies divide over 32
+// threads with at most 16 elements per thread
+template <int N>
+constexpr bool warp_plan_ok() {
+  using Rad = typename Plan<N>::R;
+  for (int p = 0; p < Rad::count; ++p)
+    if ((N / Rad::value[p]) % 32 != 0) return false;
+  return N / 32 <= 16;
+}
+template <int N, int W>
+constexpr bool warpcol_ok() {
+  return warp_plan_ok<N>() && W <= N && N % W == 0 && W % 2 == 0 && WarpCfg<N, W>::NT <= 1024 &&
+         WarpCfg<N, W>::SMEM <= kMaxSmem;
+}
 constexpr int kColWidths[3] = {4, 8, 16};
 constexpr int kRowWidths[5] = {1, 2, 4, 8, 16};
 
@@ -154,11 +168,30 @@ cudaError_t launch_cols_pair(const Ctx& c) {
   return cudaGetLastError();
 }
 
+template <int N, int W>
+cudaError_t launch_cols_warp(const Ctx& c) {
+  using P = WarpCfg<N, W>;
+  auto kern = k_cols_warp<N, W>;
+  static unsigned long long configured = 0ull;
+  static int resident[64] = {0};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / W);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
+  const int grid = tiles < slots ? tiles : slots;
+  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.ipp, c.first, c.count, c.tw);
+  return cudaGetLastError();
+}
+
 // column-pass variant code: W > 0 one column per thread, W columns per tile;
-// W < 0 two columns per thread, -W columns per tile
+// W < 0 two columns per thread, -W columns per tile; 100 + W one warp per
+// column, W columns per tile
 template <int N>
 cudaError_t launch_cols_w(const Ctx& c, int w) {
   switch (w) {
+    case 104: if constexpr (warpcol_ok<N, 4>()) return launch_cols_warp<N, 4>(c); break;
+    case 108: if constexpr (warpcol_ok<N, 8>()) return launch_cols_warp<N, 8>(c); break;
+    case 116: if constexpr (warpcol_ok<N, 16>()) return launch_cols_warp<N, 16>(c); break;
     case -4: if constexpr (pair_ok<N, 4>()) return launch_cols_pair<N, 4>(c); break;
     case -8: if constexpr (pair_ok<N, 8>()) return launch_cols_pair<N, 8>(c); break;
     case -16: if constexpr (pair_ok<N, 16>()) return launch_cols_pair<N, 16>(c); break;
@@ -258,6 +291,9 @@ struct SizeImpl {
 
   static int col_widths(int* out) {
     int k = 0;
+    if constexpr (warpcol_ok<N, 4>()) out[k++] = 104;
+    if constexpr (warpcol_ok<N, 8>()) out[k++] = 108;
+    if constexpr (warpcol_ok<N, 16>()) out[k++] = 116;
     if constexpr (pair_ok<N, 4>()) out[k++] = -4;
     if constexpr (pair_ok<N, 8>()) out[k++] = -8;
     if constexpr (pair_ok<N, 16>()) out[k++] = -16;

@@ -1,7 +1,8 @@
 """Tile-width variants of the iteration kernels and the autotuner.
 
 Every compiled tile width -- including the column pass that keeps two
-columns per thread (negative widths) -- performs the same per-element
+columns per thread (negative widths) and the one with a warp per column
+(100 + width) -- performs the same per-element
 arithmetic, so all variants must give bit-identical results; the autotuner
 must leave the population as it found it."""
 import itertools
@@ -30,7 +31,7 @@ def test_all_tile_widths_bit_identical(n):
     e, dens, S = engine(n, P)
     ref = None
     tried = 0
-    for wc, wr in itertools.product([4, 8, 16, -4, -8, -16], [1, 2, 4, 8, 16]):
+    for wc, wr in itertools.product([4, 8, 16, -4, -8, -16, 104, 108, 116], [1, 2, 4, 8, 16]):
         try:
             e.set_tiles(wc, wr)
         except _lib.EngineError:
