@@ -36,6 +36,9 @@ N = 512
 POP = 64
 BETA = 0.87
 B_PER_PIXEL_ITER = 24  # rho read+write 16 B, amplitude 4 B, support 4 B
+# DRAM bytes of one iteration (column pass + row pass) at 512^2 x 64, from
+# the committed ncu captures: 135.3 + 78.7 + 335.6 + 207.8 MB
+ITER_DRAM_BYTES = 757_400_000
 
 
 def parse():
@@ -53,6 +56,8 @@ def parse():
                     help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
     ap.add_argument("--batch-patterns", type=int, default=256,
                     help="patterns of uneven sizes in the graph-captured batch (0: skip)")
+    ap.add_argument("--refine", type=int, default=1, help="time the gradient-refinement epoch (0: skip)")
+    ap.add_argument("--profile-loss", action="store_true", help="profiling case: one loss + gradient at 512^2 x 64")
     ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
     ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
@@ -311,6 +316,66 @@ def batched_sizes(args, local):
     return out
 
 
+def refinement(args, local):
+    """Gradient refinement workload: 1024 x 1024, 32 individuals; an epoch is
+    100 HIO iterations then 50 Adam steps on the Poisson loss through the
+    hand-written loss / adjoint kernels (FarFieldLoss).  Also the time of one
+    loss + gradient evaluation (forward and backward) and its bandwidth on
+    24 algorithmic bytes per pixel (density and support read, amplitude,
+    gradient written)."""
+    import torch
+    from s_spi_spring_gb300 import _lib, synthetic
+    from s_spi_spring_gb300.refine import FarFieldLoss, population_tensors, refine
+    n, P = 1024, 32
+    dev = torch.device("cuda", local)
+    I, _, _ = synthetic.polygon_pattern(seed=3, n=n, diameter=240.0, photons=1e8, stop_radius=8, gap=4, stripes=2)
+    eng = _lib.Engine(n, local)
+    stream = torch.cuda.current_stream(dev)
+    eng.set_stream(stream.cuda_stream or 1)  # torch's stream (1: the legacy default stream)
+    eng.set_amplitudes(_lib.prepare_pattern(I, (-1, -1), True))
+    dens, S = synthetic.start_population(n, P, 220.0, seed=4)
+    eng.upload(0, dens, S)
+    eng.hio(0, P, 20, 0.9, 0.0)
+    d, s = population_tensors(eng, 0, P, dev)
+
+    def loss_grad():
+        x = d.detach().requires_grad_(True)
+        FarFieldLoss.apply(x, s, eng, "poisson", 1e-6).sum().backward()
+        return x.grad
+
+    for _ in range(3):
+        loss_grad()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record(stream)
+    for _ in range(reps):
+        loss_grad()
+    e1.record(stream)
+    e1.synchronize()
+    lg_ms = e0.elapsed_time(e1) / reps
+    alg = 24 * P * n * n
+    peak, kind = peaks()
+    # one epoch: HIO 100 + Adam 50 (after one short untimed epoch: the
+    # optimiser's kernels load on first use)
+    refine(eng, 0, P, steps=2, lr=1e-3, loss="poisson", eps=1e-6, device=dev)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    eng.hio(0, P, 100, 0.9, 0.0)
+    hist = refine(eng, 0, P, steps=50, lr=1e-3, loss="poisson", eps=1e-6, device=dev)
+    e1.record(stream)
+    e1.synchronize()
+    ep_ms = e0.elapsed_time(e1)
+    m = eng.evaluate(0, P)
+    eng.close()
+    return {"workload": "1024x1024 complex64, 32 individuals; epoch = 100 HIO + 50 Adam steps (Poisson loss)",
+            "ms_per_epoch": round(ep_ms, 2), "loss_grad_ms": round(lg_ms, 3),
+            "loss_grad_gbps": round(alg / (lg_ms / 1e3) / 1e9, 1),
+            "loss_grad_frac": round(alg / (lg_ms / 1e3) / 1e9 / peak, 4), "peak_source": kind,
+            "loss_first_last": [round(hist[0], 1), round(hist[-1], 1)],
+            "rfactor_median": round(float(np.median([x["error_fourier"] for x in m])), 5)}
+
+
 def run_engine(args):
     import torch
     from s_spi_spring_gb300 import _lib
@@ -426,7 +491,10 @@ def run_engine(args):
                 "h2d_bytes_per_step": int(h_dens.numel() * 4 + h_supp.numel() * 4),
                 "d2h_bytes_per_step": int(h_out.numel() * 4)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "frac": round(achieved / peak, 4), "traffic": ITER_DRAM_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one column pass and "
+                                       "one row pass (profiles/k_cols_project_raar512_pop64.md, "
+                                       "profiles/k_rows_iterate_raar512_pop64.md)",
                      "kernel": "fused iteration (column pass + row pass), per iteration",
                      "alg_bytes_per_launch": alg_bytes, "ms_per_iteration": round(t_iter_ms, 5),
                      "peak_source": peak_kind},
@@ -444,6 +512,11 @@ def run_engine(args):
             out["batched_sizes"] = batched_sizes(args, local)
         except Exception as ex:
             out["batched_sizes"] = {"error": str(ex)[:300]}
+    if rank == 0 and args.refine:
+        try:
+            out["refinement"] = refinement(args, local)
+        except Exception as ex:
+            out["refinement"] = {"error": str(ex)[:300]}
     if rank == 0 and args.memetic_gens > 0:
         try:
             out["memetic"] = memetic(args, local, tiles, sched)
@@ -521,6 +594,24 @@ def configure(eng, args, tune_iters=10):
     return eng.tiles(), eng.schedule()
 
 
+def run_profile_loss():
+    """One Poisson loss + gradient on the resident workload (for ncu)."""
+    import torch
+    from s_spi_spring_gb300 import _lib
+    from s_spi_spring_gb300.refine import FarFieldLoss, population_tensors
+    A, dens, S = workload()
+    eng = _lib.Engine(N, 0)
+    eng.set_stream(torch.cuda.current_stream().cuda_stream or 1)
+    eng.set_amplitudes(A)
+    eng.upload(0, dens, S)
+    d, s = population_tensors(eng, 0, POP, torch.device("cuda", 0))
+    for _ in range(2):
+        x = d.detach().requires_grad_(True)
+        FarFieldLoss.apply(x, s, eng, "poisson", 1e-6).sum().backward()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "loss+gradient", "n": N, "population": POP}))
+
+
 def run_profile_case(args):
     """One RAAR call on the resident workload (for ncu captures)."""
     from s_spi_spring_gb300 import _lib
@@ -542,6 +633,9 @@ def main():
     args = parse()
     if args.profile_iters > 0:
         run_profile_case(args)
+        return
+    if args.profile_loss:
+        run_profile_loss()
         return
     if args.impl == "reference":
         run_reference(args)

@@ -286,6 +286,18 @@ int spe_graph_end(void* stream, spe_graph** out);
 int spe_graph_launch(spe_graph* g, void* stream);
 int spe_graph_destroy(spe_graph* g);
 
+/* One step of gradient refinement fused on the device (no reference
+ * counterpart): the loss of spe_loss_grad at the current densities into
+ * loss_out (device, count doubles, may be NULL), then one Adam step of
+ * torch.optim.Adam's arithmetic (no weight decay; complex values as pairs of
+ * reals) applied in place to `density`, with the first and second moments
+ * in exp_avg / exp_avg_sq (device, complex64 layout, count*n*n each, zero
+ * before step 1).  `step` counts from 1.  The gradient never reaches memory:
+ * the last pass of the adjoint applies the update. */
+int spe_adam_step(spe_engine* e, void* density, const int32_t* support, void* exp_avg, void* exp_avg_sq, int count,
+                  int loss, float eps, float lr, float beta1, float beta2, float adam_eps, int step,
+                  double* loss_out);
+
 /* Iteration schedule (no reference counterpart; the reference runs one
  * individual per context): HIO / RAAR / ER calls process the range in blocks
  * of `chunk` individuals (0: the whole range at once), each block through

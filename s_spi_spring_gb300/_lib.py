@@ -79,6 +79,7 @@ SIGNATURES = {
     "spe_gather": (_i, [_vp, _ip, _i, _i]),
     "spe_loss_grad": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp, _vp]),
     "spe_set_amplitudes_batch": (_i, [_vp, _fp, _i, _i]),
+    "spe_adam_step": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _f, _f, _f, _f, _i, _vp]),
     "spe_get_rng_state": (_i, [_vp, C.c_char_p, _i, C.POINTER(_i)]),
     "spe_set_rng_state": (_i, [_vp, C.c_char_p]),
     "spe_stream_create": (_i, [C.POINTER(_vp)]),
@@ -353,6 +354,13 @@ class Engine:
         """Far-field loss / gradient on device arrays given by address."""
         call("spe_loss_grad", self.h, _vp(density_ptr), _vp(support_ptr), int(count), int(loss), float(eps),
              _vp(loss_ptr or 0), _vp(grad_ptr or 0), _vp(scale_ptr or 0))
+
+    def adam_step(self, density_ptr, support_ptr, m_ptr, v_ptr, count, loss=1, eps=0.0, lr=1e-3, beta1=0.9,
+                  beta2=0.999, adam_eps=1e-8, step=1, loss_ptr=0):
+        """Loss at the current densities, then one fused Adam step in place."""
+        call("spe_adam_step", self.h, _vp(density_ptr), _vp(support_ptr), _vp(m_ptr), _vp(v_ptr), int(count),
+             int(loss), float(eps), float(lr), float(beta1), float(beta2), float(adam_eps), int(step),
+             _vp(loss_ptr or 0))
 
     def population_arrays(self, first, count):
         """Device addresses of slots [first, first+count): (density, support)."""

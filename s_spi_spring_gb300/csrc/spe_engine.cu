@@ -303,7 +303,9 @@ int run_iterations(spe_engine* e, int first, int count, int upd, int iters, floa
   return SPE_OK;
 }
 
-size_t max_tiles(const spe::SizeOps* o) { return (size_t)std::max(o->tiles_rows, o->tiles_cols); }
+size_t max_tiles(const spe::SizeOps* o) {
+  return (size_t)std::max(std::max(o->tiles_rows, o->tiles_cols), o->loss_tiles);
+}
 size_t region(spe_engine* e) { return (size_t)e->cap * max_tiles(e->ops) * spe::NRED; }
 
 // tpi: CTAs per individual of the pass that wrote the partials
@@ -744,7 +746,7 @@ int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, in
   c.S = const_cast<int*>(support);
   CK(e->ops->loss_grad(c, loss, eps, e->partials, static_cast<float2*>(grad_out), grad_scale), "loss kernels");
   if (loss_out) {
-    if ((rc = reduce(e, e->partials, count, e->ops->tiles_cols, 0, 0, 0))) return rc;
+    if ((rc = reduce(e, e->partials, count, e->ops->loss_tiles, 0, 0, 0))) return rc;
     CK(cudaMemcpy2DAsync(loss_out, sizeof(double), e->red, 16 * sizeof(double), sizeof(double), count,
                          cudaMemcpyDeviceToDevice, e->st),
        "loss copy");
@@ -808,6 +810,38 @@ int spe_graph_destroy(spe_graph* g) {
   cudaGraphExecDestroy(g->exec);
   cudaGraphDestroy(g->graph);
   delete g;
+  return SPE_OK;
+}
+
+int spe_adam_step(spe_engine* e, void* density, const int32_t* support, void* exp_avg, void* exp_avg_sq, int count,
+                  int loss, float eps, float lr, float beta1, float beta2, float adam_eps, int step,
+                  double* loss_out) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  int rc = need_amp(e);
+  if (rc) return rc;
+  if (count < 0 || step < 1) return fail(SPE_ERR_INVALID, "negative count or step < 1");
+  if (loss != SPE_LOSS_AMPLITUDE && loss != SPE_LOSS_POISSON) return fail(SPE_ERR_INVALID, "unknown loss %d", loss);
+  if (!(eps >= 0.f) || !(lr >= 0.f) || !(beta1 >= 0.f && beta1 < 1.f) || !(beta2 >= 0.f && beta2 < 1.f) ||
+      !(adam_eps > 0.f))
+    return fail(SPE_ERR_INVALID, "invalid optimiser parameters");
+  if (count == 0) return SPE_OK;
+  if (!density || !support || !exp_avg || !exp_avg_sq) return fail(SPE_ERR_INVALID, "null device array");
+  if ((rc = spe_reserve(e, count))) return rc;
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  // torch.optim.Adam's bias corrections, in double
+  const double bc1 = 1.0 - std::pow((double)beta1, step), bc2 = 1.0 - std::pow((double)beta2, step);
+  spe::Ctx c = make_ctx(e, 0, count);
+  c.rho = static_cast<float2*>(density);
+  c.S = const_cast<int*>(support);
+  CK(e->ops->adam_step(c, loss, eps, e->partials, static_cast<float2*>(exp_avg), static_cast<float2*>(exp_avg_sq),
+                       beta1, beta2, (float)(lr / bc1), (float)(1.0 / std::sqrt(bc2)), adam_eps),
+     "refinement kernels");
+  if (loss_out) {
+    if ((rc = reduce(e, e->partials, count, e->ops->loss_tiles, 0, 0, 0))) return rc;
+    CK(cudaMemcpy2DAsync(loss_out, sizeof(double), e->red, 16 * sizeof(double), sizeof(double), count,
+                         cudaMemcpyDeviceToDevice, e->st),
+       "loss copy");
+  }
   return SPE_OK;
 }
 

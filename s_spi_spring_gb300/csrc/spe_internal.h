@@ -110,6 +110,11 @@ struct SizeOps {
   // Ctx::rho / Ctx::S into column-pass partials; with grad, the adjoint
   // gradient times scale[item] (scale may be null)
   cudaError_t (*loss_grad)(const Ctx&, int loss, float eps, double* partials, float2* grad, const float* scale);
+  int loss_tiles;  // loss partials per item
+  // loss at the current densities into partials, then one Adam step in
+  // place with moments m, v (see OpRowsGradAdam)
+  cudaError_t (*adam_step)(const Ctx&, int loss, float eps, double* partials, float2* m, float2* v, float b1,
+                           float b2, float step_size, float inv_sqrt_bc2, float adam_eps);
 };
 
 const SizeOps* size_ops(int n);

@@ -705,6 +705,40 @@ struct OpRowsGradOut : OpBase {
   }
 };
 
+// row pass: T -> FFT- (x) = the gradient G (inside the support) -> one Adam
+// step on the item's density, per real component, with the moments m, v:
+//   m += (1 - b1) (G - m);  v = b2 v + (1 - b2) G^2
+//   rho -= step_size * m / (sqrt(v) / sqrt_bc2 + eps)
+// (step_size = lr / (1 - b1^t), sqrt_bc2 = sqrt(1 - b2^t): torch.optim.Adam
+// without weight decay, complex parameters as pairs of reals)
+struct OpRowsGradAdam : OpBase {
+  static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 0, NMAX = 0;
+  const float2* T;
+  const int* S;
+  float2* rho;
+  float2* m;
+  float2* v;
+  float b1, b2, step_size, inv_sqrt_bc2, eps;
+  using Acc = NoAcc;
+  __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
+  __device__ float2 mid(float2 x, size_t, int, int, int, Acc&) const { return x; }
+  __device__ __forceinline__ float upd(float g, float& mm, float& vv, float p) const {
+    mm = mm + (1.f - b1) * (g - mm);
+    vv = vv * b2 + (1.f - b2) * g * g;
+    const float den = sqrtf(vv) * inv_sqrt_bc2 + eps;
+    return p - step_size * (mm / den);
+  }
+  __device__ void store(float2 g, size_t gi, int, int, int, Acc&) const {
+    if (S[gi] <= 0) g = make_float2(0.f, 0.f);
+    float2 mm = m[gi], vv = v[gi], p = rho[gi];
+    p.x = upd(g.x, mm.x, vv.x, p.x);
+    p.y = upd(g.y, mm.y, vv.y, p.y);
+    m[gi] = mm;
+    v[gi] = vv;
+    rho[gi] = p;
+  }
+};
+
 // ---- generic 2D transforms on arrays of items (item p at offset p*N*N)
 
 // column pass: src -> FFT(S) (y) -> dst

@@ -87,6 +87,17 @@ __device__ __forceinline__ void load_twiddles(float2* tw, const float2* __restri
   for (int i = threadIdx.x; i < TWS; i += nt) tw[i] = twg[i];
 }
 
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream serialisation attribute may start while the previous kernel of the
+// stream drains.  It lets its own dependents start early, loads what no
+// kernel writes (the twiddle tables), then waits until the previous grid has
+// completed and its writes are visible before touching the population.
+// Without the attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // column pass: T -> FFT+ (y) -> P_M with A -> FFT- (y) -> T
 template <int N, int W>
 __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
@@ -98,7 +109,9 @@ __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
   extern __shared__ __align__(128) unsigned char sm[];
   float2* tw = reinterpret_cast<float2*>(sm);
   unsigned char* stages = sm + C::TWB;
+  pdl_enter();
   load_twiddles<N>(tw, twg, NT);
+  pdl_wait();
   const int t = threadIdx.x;
   const int c = t % W, j = t / W;
   const int ntiles = count * TPI;
@@ -152,6 +165,92 @@ __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
   }
 }
 
+// column pass of the far-field loss: T -> FFT+ (y) = F -> loss terms over
+// the known pixels (one FP64 sum per tile into partials[tile]); with GRAD,
+// F -> 2 dL/dconj(F) -> FFT- (y) -> T.  Same staging and pipeline as the
+// column pass of the iteration.
+template <int N, int W, int LOSS, bool GRAD>
+__global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
+    k_cols_loss(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count, float eps,
+                double* __restrict__ partials, const float2* __restrict__ twg) {
+  using C = ColCfg<N, W>;
+  constexpr int NT = C::NT, E = C::E, TPI = N / W, NW = NT / 32;
+  using Lay = LayCol<N, W>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ double red[NW];
+  float2* tw = reinterpret_cast<float2*>(sm);
+  unsigned char* stages = sm + C::TWB;
+  pdl_enter();
+  load_twiddles<N>(tw, twg, NT);
+  pdl_wait();
+  const int t = threadIdx.x;
+  const int c = t % W, j = t / W;
+  const int ntiles = count * TPI;
+
+  auto stage_tile = [&](int tile, int s) {
+    const int p = first + tile / TPI;
+    const int x0 = (tile % TPI) * W;
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::STAGE);
+    float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
+    const float2* gT = T + (size_t)p * N * N + x0;
+    const float* Ap = ipp > 0 ? A + (size_t)(p / ipp) * N * N : A;
+    for (int q = t; q < N * W / 2; q += NT) {
+      const int y = q / (W / 2), h = q - y * (W / 2);
+      cp_async16(&sT[Lay::idx(y, 2 * h)], gT + (size_t)y * N + 2 * h);
+    }
+    for (int q = t; q < N * W / 4; q += NT) {
+      const int y = q / (W / 4), h = q - y * (W / 4);
+      cp_async16(&sA[y * W + 4 * h], Ap + (size_t)y * N + x0 + 4 * h);
+    }
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) stage_tile(tile, 0);
+  cp_async_commit();
+  for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) stage_tile(nxt, (k + 1) & 1);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    const int s = k & 1;
+    float2* sT = reinterpret_cast<float2*>(stages + s * C::STAGE);
+    const float* sA = reinterpret_cast<const float*>(stages + s * C::STAGE + C::C_T);
+    const int p = first + tile / TPI;
+    const int x = (tile % TPI) * W + c;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = sT[Lay::idx(elem_pos<N>(e, j), c)];
+    __syncthreads();  // the stage's T region becomes the exchange buffer
+    fft_reg<N, Lay, +1>(v, sT, tw, c, j);
+    float acc = 0.f;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const float a = sA[elem_pos<N>(e, j) * W + c];
+      float2 g = make_float2(0.f, 0.f);
+      if (a >= 0.f) acc += loss_term<LOSS>(v[e], a, eps, GRAD ? &g : nullptr);
+      v[e] = g;
+    }
+    if (GRAD) {
+      fft_reg<N, Lay, -1>(v, sT, tw, c, j);
+      float2* gT = T + (size_t)p * N * N + x;
+#pragma unroll
+      for (int e = 0; e < E; ++e) gT[(size_t)elem_pos<N>(e, j) * N] = v[e];
+    }
+    // the tile's FP64 sum
+    double d = acc;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) d += __shfl_down_sync(0xffffffffu, d, off);
+    if ((t & 31) == 0) red[t >> 5] = d;
+    __syncthreads();  // (also: stage s is refilled by the next iteration's prefetch)
+    if (t == 0) {
+      double a = red[0];
+      for (int w = 1; w < NW; ++w) a += red[w];
+      partials[(size_t)tile * NRED] = a;
+    }
+  }
+}
+
 // row pass: T -> FFT- (x) -> /N^2 -> update with (rho, S) -> rho -> FFT+ (x) -> T
 template <int N, int W, int UPD>
 __global__ void __launch_bounds__(RowCfg<N, W>::NT, RowCfg<N, W>::MINB)
@@ -164,7 +263,9 @@ __global__ void __launch_bounds__(RowCfg<N, W>::NT, RowCfg<N, W>::MINB)
   float2* tw = reinterpret_cast<float2*>(sm);
   float2* xb = reinterpret_cast<float2*>(sm + C::TWB);
   unsigned char* stages = sm + C::TWB + C::R_X;
+  pdl_enter();
   load_twiddles<N>(tw, twg, NT);
+  pdl_wait();
   const int t = threadIdx.x;
   const int j = t % TPT, c = t / TPT;
   const int ntiles = count * TPI;
@@ -335,7 +436,9 @@ __global__ void __launch_bounds__(PairCfg<N, WP>::NT, PairCfg<N, WP>::MINB)
   extern __shared__ __align__(128) unsigned char sm[];
   float2* tw = reinterpret_cast<float2*>(sm);
   unsigned char* stages = sm + C::TWB;
+  pdl_enter();
   load_twiddles<N>(tw, twg, NT);
+  pdl_wait();
   const int t = threadIdx.x;
   const int h = t % WP, j = t / WP;
   const int ntiles = count * TPI;
@@ -439,7 +542,9 @@ __global__ void __launch_bounds__(WarpCfg<N, W>::NT, WarpCfg<N, W>::MINB)
   extern __shared__ __align__(128) unsigned char sm[];
   float2* tw = reinterpret_cast<float2*>(sm);
   unsigned char* stages = sm + C::TWB;
+  pdl_enter();
   load_twiddles<N>(tw, twg, NT);
+  pdl_wait();
   const int t = threadIdx.x;
   const int c = t >> 5, j = t & 31;
   const int ntiles = count * TPI;

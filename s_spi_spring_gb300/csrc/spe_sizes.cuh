@@ -117,6 +117,23 @@ int resident_ctas(K kern, int threads, size_t smem, int* cache) {
   return cache[dev];
 }
 
+// launch with programmatic stream serialisation (the kernel's prologue
+// overlaps the previous kernel's drain; see pdl_wait)
+template <class K, class... Args>
+cudaError_t launch_pdl(K kern, int grid, int threads, size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // the resident CTAs a persistent launch takes when `div` kernels share the GPU
 inline int share(int slots, int div) {
   const int s = div > 1 ? slots / div : slots;
@@ -134,8 +151,7 @@ cudaError_t launch_cols_project(const Ctx& c) {
   const int tiles = c.count * (N / W);
   const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
-  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.ipp, c.first, c.count, c.tw);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, c.tw);
 }
 
 template <int N, int W, int UPD>
@@ -149,8 +165,8 @@ cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
   const int tiles = c.count * (N / W);
   const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
-  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.rho, c.S, c.first, c.count, scale, beta, g, c.tw);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.rho, static_cast<const int*>(c.S), c.first, c.count,
+                    scale, beta, g, c.tw);
 }
 
 template <int N, int W>
@@ -164,8 +180,7 @@ cudaError_t launch_cols_pair(const Ctx& c) {
   const int tiles = c.count * (N / W);
   const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
-  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.ipp, c.first, c.count, c.tw);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, c.tw);
 }
 
 template <int N, int W>
@@ -179,8 +194,21 @@ cudaError_t launch_cols_warp(const Ctx& c) {
   const int tiles = c.count * (N / W);
   const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
   const int grid = tiles < slots ? tiles : slots;
-  kern<<<grid, P::NT, P::SMEM, c.st>>>(c.T, c.A, c.ipp, c.first, c.count, c.tw);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, c.tw);
+}
+
+template <int N, int W, int LOSS, bool GRAD>
+cudaError_t launch_cols_loss(const Ctx& c, float eps, double* partials) {
+  using P = ColCfg<N, W>;
+  auto kern = k_cols_loss<N, W, LOSS, GRAD>;
+  static unsigned long long configured = 0ull;
+  static int resident[64] = {0};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / W);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
+  const int grid = tiles < slots ? tiles : slots;
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, eps, partials, c.tw);
 }
 
 // column-pass variant code: W > 0 one column per thread, W columns per tile;
@@ -516,26 +544,9 @@ struct SizeImpl {
     rf.S = c.S;
     rf.T = c.T;
     SPE_TRY((launch_pass<N, AX_ROWS>(rf, c.count, c.st, c.tw)));
-    if (!grad) {
-      OpColsLoss<LOSS, false> cl;
-      cl.first = c.first;
-      cl.partials = partials;
-      cl.T = c.T;
-      cl.A = c.A;
-      cl.n = N;
-      cl.ipp = c.ipp;
-      cl.eps = eps;
-      return launch_pass<N, AX_COLS>(cl, c.count, c.st, c.tw);
-    }
-    OpColsLoss<LOSS, true> cg;
-    cg.first = c.first;
-    cg.partials = partials;
-    cg.T = c.T;
-    cg.A = c.A;
-    cg.n = N;
-    cg.ipp = c.ipp;
-    cg.eps = eps;
-    SPE_TRY((launch_pass<N, AX_COLS>(cg, c.count, c.st, c.tw)));
+    constexpr int WL = DefaultTiles<N>::cols;  // loss partials: N / WL per item
+    if (!grad) return launch_cols_loss<N, WL, LOSS, false>(c, eps, partials);
+    SPE_TRY((launch_cols_loss<N, WL, LOSS, true>(c, eps, partials)));
     OpRowsGradOut go;
     go.first = c.first;
     go.partials = nullptr;
@@ -545,6 +556,41 @@ struct SizeImpl {
     go.scale = scale;
     return launch_pass<N, AX_ROWS>(go, c.count, c.st, c.tw);
   }
+  // loss (partials) at the current densities, then one Adam step in place
+  template <int LOSS>
+  static cudaError_t adam_step_t(const Ctx& c, float eps, double* partials, float2* m, float2* v, float b1, float b2,
+                                 float step_size, float inv_sqrt_bc2, float adam_eps) {
+    OpRowsSupportForward rf;
+    rf.first = c.first;
+    rf.partials = nullptr;
+    rf.rho = c.rho;
+    rf.S = c.S;
+    rf.T = c.T;
+    SPE_TRY((launch_pass<N, AX_ROWS>(rf, c.count, c.st, c.tw)));
+    constexpr int WL = DefaultTiles<N>::cols;
+    SPE_TRY((launch_cols_loss<N, WL, LOSS, true>(c, eps, partials)));
+    OpRowsGradAdam ad;
+    ad.first = c.first;
+    ad.partials = nullptr;
+    ad.T = c.T;
+    ad.S = c.S;
+    ad.rho = c.rho;
+    ad.m = m;
+    ad.v = v;
+    ad.b1 = b1;
+    ad.b2 = b2;
+    ad.step_size = step_size;
+    ad.inv_sqrt_bc2 = inv_sqrt_bc2;
+    ad.eps = adam_eps;
+    return launch_pass<N, AX_ROWS>(ad, c.count, c.st, c.tw);
+  }
+  static cudaError_t adam_step(const Ctx& c, int loss, float eps, double* partials, float2* m, float2* v, float b1,
+                               float b2, float step_size, float inv_sqrt_bc2, float adam_eps) {
+    return loss == LOSS_POISSON
+               ? adam_step_t<LOSS_POISSON>(c, eps, partials, m, v, b1, b2, step_size, inv_sqrt_bc2, adam_eps)
+               : adam_step_t<LOSS_AMPLITUDE>(c, eps, partials, m, v, b1, b2, step_size, inv_sqrt_bc2, adam_eps);
+  }
+
   static cudaError_t loss_grad(const Ctx& c, int loss, float eps, double* partials, float2* grad,
                                const float* scale) {
     return loss == LOSS_POISSON ? loss_grad_t<LOSS_POISSON>(c, eps, partials, grad, scale)
@@ -571,7 +617,9 @@ struct SizeImpl {
                               DefaultTiles<N>::cols,
                               DefaultTiles<N>::rows,
                               &SizeImpl<N>::known_power,
-                              &SizeImpl<N>::loss_grad};
+                              &SizeImpl<N>::loss_grad,
+                              N / DefaultTiles<N>::cols,
+                              &SizeImpl<N>::adam_step};
     return &t;
   }
 };

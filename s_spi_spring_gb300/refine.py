@@ -8,8 +8,11 @@ applies the adjoint through FFT, mask and support.  Bulk arithmetic is FP32;
 the per-individual loss sums are FP64.
 
 ``refine`` runs Adam on individuals that stay in the engine's population
-slots: the optimiser's parameter is a tensor that aliases the engine's
-device memory, so refinement and iteration share the data without copies.
+slots: the optimiser works on a tensor that aliases the engine's device
+memory, so refinement and iteration share the data without copies.  By
+default each step is fused on the device (``spe_adam_step``: loss, adjoint,
+and the Adam update inside the adjoint's last pass); the autograd path
+(``fused=False``) runs the same arithmetic through torch.optim.Adam.
 """
 from __future__ import annotations
 
@@ -86,15 +89,32 @@ def farfield_loss(density, support, engine, loss="amplitude", eps=0.0):
     return FarFieldLoss.apply(density, support, engine, loss, eps)
 
 
-def refine(engine, first, count, steps=50, lr=1e-3, loss="poisson", eps=1e-6, device=None):
+def refine(engine, first, count, steps=50, lr=1e-3, loss="poisson", eps=1e-6, device=None, fused=True,
+           betas=(0.9, 0.999), adam_eps=1e-8):
     """Adam on individuals [first, first+count) of `engine`'s population, in
     place: `steps` steps on the summed per-individual loss.  Returns the
-    per-step loss sums (on the host at the end)."""
+    per-step loss sums (on the host at the end).
+
+    fused=True runs each step as three passes on the device (loss, adjoint,
+    and the Adam update applied by the adjoint's last pass: spe_adam_step);
+    fused=False runs FarFieldLoss through torch autograd and
+    torch.optim.Adam -- the same arithmetic, the gradient going through
+    memory and the optimiser's own kernels."""
     device = device or torch.device("cuda", torch.cuda.current_device())
     dens, supp = population_tensors(engine, first, count, device)
-    param = torch.nn.Parameter(dens)  # shares the engine's memory
-    opt = torch.optim.Adam([param], lr=lr)
     history = []
+    if fused:
+        _bind_stream(engine, device)
+        m = torch.zeros_like(dens)
+        v = torch.zeros_like(dens)
+        losses = torch.empty((steps, count), dtype=torch.float64, device=device)
+        for t in range(steps):
+            engine.adam_step(dens.data_ptr(), supp.data_ptr(), m.data_ptr(), v.data_ptr(), count, LOSSES[loss], eps,
+                             lr, betas[0], betas[1], adam_eps, t + 1, losses[t].data_ptr())
+        torch.cuda.synchronize(device)
+        return losses.sum(dim=1).tolist()
+    param = torch.nn.Parameter(dens)  # shares the engine's memory
+    opt = torch.optim.Adam([param], lr=lr, betas=betas, eps=adam_eps)
     for _ in range(steps):
         opt.zero_grad(set_to_none=True)
         total = FarFieldLoss.apply(param, supp, engine, loss, eps).sum()

@@ -94,3 +94,13 @@ def test_crossover_draws_match_oracle(seed, P, crossft, crossexp):
         assert np.array_equal(cm[off:off + d.crossmap.size], d.crossmap)
         off += d.crossmap.size
     assert off == cm.size
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No silent fallback: without the compiled engine every entry raises."""
+    monkeypatch.setattr(_lib, "_LIB_PATH", tmp_path / "libspe_missing.so")
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(ImportError):
+        _lib.load()
+    with pytest.raises(ImportError):
+        _lib.Engine(64, 0)
