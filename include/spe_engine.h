@@ -298,6 +298,37 @@ int spe_adam_step(spe_engine* e, void* density, const int32_t* support, void* ex
                   int loss, float eps, float lr, float beta1, float beta2, float adam_eps, int step,
                   double* loss_out);
 
+/* Detector-image preprocessing (the spring_core.pattern module,
+ * src/pattern/pattern.cpp, bindings src/wrapper.cpp:318-449), on the GPU.
+ * Host arrays of doubles, row-major with x fastest: `w` pixels per row, `h`
+ * rows.  spe_pattern_resample splats every input pixel bilinearly onto a
+ * new_w x new_h grid and normalises by the accumulated weight; pixels whose
+ * weight stays below 0.1 of the reference weight become -1:
+ *   SPE_RESAMPLE_PLAIN     Pattern::downscale: pixels >= 0, both axes scaled
+ *                          by w/new_w (as the reference does), mask unused
+ *   SPE_RESAMPLE_EWALD     Pattern::downscale_and_correct: pixels with
+ *                          mask > 0.5, Ewald-sphere mapping about (cx, cy),
+ *                          intensities divided by cos^3 of the angle
+ *   SPE_RESAMPLE_CUT_EWALD Pattern::cut_downscale_and_correct: the same
+ *                          mapping onto a centred cut of cut_w x cut_h
+ *                          input pixels; out_mask receives the resampled mask
+ *   SPE_RESAMPLE_CUT       Pattern::cut_and_downscale: centred cut without
+ *                          the correction; out_mask as above
+ * distance and pixel_size (same unit) are used by the Ewald variants. */
+enum { SPE_RESAMPLE_PLAIN = 0, SPE_RESAMPLE_EWALD = 1, SPE_RESAMPLE_CUT_EWALD = 2, SPE_RESAMPLE_CUT = 3 };
+int spe_pattern_resample(int mode, const double* data, const double* mask, int w, int h, double cx, double cy,
+                         double distance, double pixel_size, int cut_w, int cut_h, int new_w, int new_h,
+                         double* out_data, double* out_mask, int device);
+
+/* Pattern::get_radial_profile: for increasing `angles`, the average of the
+ * pixels >= 0 whose scattering angle (distance from (cx, cy) times dtheta)
+ * falls between neighbouring angles, split linearly between the two, over
+ * the directions [phi_min, phi_max] in degrees; bins with a total weight
+ * of 4 or less are -1. */
+int spe_pattern_radial_profile(const double* data, int w, int h, double dtheta, double cx, double cy,
+                               const double* angles, int nangles, double phi_min, double phi_max, double* out,
+                               int device);
+
 /* Iteration schedule (no reference counterpart; the reference runs one
  * individual per context): HIO / RAAR / ER calls process the range in blocks
  * of `chunk` individuals (0: the whole range at once), each block through

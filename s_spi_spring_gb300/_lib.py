@@ -19,6 +19,7 @@ _lib = None
 SPE_OK = 0
 SPE_OP_HIO, SPE_OP_RAAR, SPE_OP_ER, SPE_OP_SW, SPE_OP_SWA = range(5)
 SPE_LOSS_AMPLITUDE, SPE_LOSS_POISSON = 0, 1
+SPE_RESAMPLE_PLAIN, SPE_RESAMPLE_EWALD, SPE_RESAMPLE_CUT_EWALD, SPE_RESAMPLE_CUT = 0, 1, 2, 3
 
 # Every symbol the header declares, with (restype, argtypes).
 _vp = C.c_void_p
@@ -82,6 +83,10 @@ SIGNATURES = {
     "spe_adam_step": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _f, _f, _f, _f, _i, _vp]),
     "spe_get_rng_state": (_i, [_vp, C.c_char_p, _i, C.POINTER(_i)]),
     "spe_set_rng_state": (_i, [_vp, C.c_char_p]),
+    "spe_pattern_resample": (_i, [_i, _vp, _vp, _i, _i, C.c_double, C.c_double, C.c_double, C.c_double, _i, _i,
+                                  _i, _i, _vp, _vp, _i]),
+    "spe_pattern_radial_profile": (_i, [_vp, _i, _i, C.c_double, C.c_double, C.c_double, _vp, _i, C.c_double,
+                                        C.c_double, _vp, _i]),
     "spe_stream_create": (_i, [C.POINTER(_vp)]),
     "spe_stream_destroy": (_i, [_vp]),
     "spe_graph_begin": (_i, [_vp]),

@@ -1,5 +1,5 @@
 """Import path of the reference's compiled module: ``spring_core.phase_retrieval``
-(reference ``src/wrapper.cpp:24-27``)."""
-from . import phase_retrieval
+and ``spring_core.pattern`` (reference ``src/wrapper.cpp:24-27, 318``)."""
+from . import pattern, phase_retrieval
 
-__all__ = ["phase_retrieval"]
+__all__ = ["pattern", "phase_retrieval"]
