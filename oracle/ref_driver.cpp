@@ -14,14 +14,20 @@
 //     records the arguments of get_new_individual;
 //   * Solver::Initialize_pop (src/solver.cpp:822-957): every draw, the disc
 //     profiles and the scaling, with a context whose transform is a
-//     double-precision DFT.
+//     double-precision DFT;
+//   * the pattern module (src/pattern/pattern.cpp): resampling and radial
+//     profiles, single-threaded so that the sums have a fixed order.
 #include <cmath>
 #include <complex>
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <tuple>
 #include <vector>
 
+#include <omp.h>
+
+#include "pattern.h"
 #include "solver.h"
 
 namespace {
@@ -173,6 +179,36 @@ int ref_crossover_draws(int n, int count, const float* errors, const int32_t* be
     used += (int)c.cmap.size();
   }
   return (int)rc->records.size() == count ? used : -1;
+}
+
+// Pattern resampling (mode as spe_pattern_resample): data / mask of w x h,
+// outputs new_w x new_h.
+int ref_pattern_resample(int mode, const double* data, const double* mask, int w, int h, double cx, double cy,
+                         double R, double dx, int cut_w, int cut_h, int new_w, int new_h, double* out, double* out_mask) {
+  omp_set_num_threads(1);
+  std::vector<double> d(data, data + (size_t)w * h);
+  std::vector<double> m;
+  if (mask) m.assign(mask, mask + (size_t)w * h);
+  Pattern p(d.data(), {(size_t)w, (size_t)h}, {cx, cy}, 1);
+  std::vector<double> r, rm;
+  const std::array<size_t, 2> nd{(size_t)new_w, (size_t)new_h}, cd{(size_t)cut_w, (size_t)cut_h};
+  if (mode == 0) r = p.downscale(nd);
+  else if (mode == 1) r = p.downscale_and_correct(R, dx, nd, m);
+  else if (mode == 2) std::tie(r, rm) = p.cut_downscale_and_correct(R, dx, cd, nd, m);
+  else std::tie(r, rm) = p.cut_and_downscale(cd, nd, m);
+  std::memcpy(out, r.data(), r.size() * sizeof(double));
+  if (!rm.empty() && out_mask) std::memcpy(out_mask, rm.data(), rm.size() * sizeof(double));
+  return 0;
+}
+
+int ref_pattern_radial_profile(const double* data, int w, int h, double dtheta, double cx, double cy,
+                               const double* angles, int nangles, double phi0, double phi1, double* out) {
+  omp_set_num_threads(1);
+  std::vector<double> d(data, data + (size_t)w * h);
+  Pattern p(d.data(), {(size_t)w, (size_t)h}, {cx, cy}, dtheta);
+  auto r = p.get_radial_profile(std::vector<double>(angles, angles + nangles), {phi0, phi1});
+  std::memcpy(out, r.data(), r.size() * sizeof(double));
+  return 0;
 }
 
 }  // extern "C"

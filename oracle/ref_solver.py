@@ -23,6 +23,14 @@ def load():
         lib.ref_crossover_draws.restype = C.c_int
         lib.ref_crossover_draws.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
                                             C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        lib.ref_pattern_resample.restype = C.c_int
+        lib.ref_pattern_resample.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double,
+                                             C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                             C.c_int, C.c_void_p, C.c_void_p]
+        lib.ref_pattern_radial_profile.restype = C.c_int
+        lib.ref_pattern_radial_profile.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                                                   C.c_double, C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                                   C.c_void_p]
         lib.ref_initialize_pop.restype = C.c_int
         lib.ref_initialize_pop.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int,
                                            C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
@@ -70,3 +78,30 @@ def initialize_pop(intensities, count, support_size, itemsize, nitems, exponent,
                            float(scaling[0]), float(scaling[1]), float(phase), int(seed), d.ctypes.data,
                            s.ctypes.data)
     return d, s
+
+
+def pattern_resample(mode, data, mask, center, R, dx, cutsize, newsize):
+    """The reference's Pattern resampling (single-threaded)."""
+    lib = load()
+    d = np.ascontiguousarray(data, dtype=np.float64)
+    h, w = d.shape
+    m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float64)
+    nw, nh = newsize
+    out = np.empty((nh, nw), np.float64)
+    om = np.empty((nh, nw), np.float64)
+    cw, ch = cutsize if cutsize is not None else (0, 0)
+    lib.ref_pattern_resample(mode, d.ctypes.data, None if m is None else m.ctypes.data, w, h, float(center[0]),
+                             float(center[1]), float(R), float(dx), int(cw), int(ch), int(nw), int(nh),
+                             out.ctypes.data, om.ctypes.data)
+    return out, om
+
+
+def pattern_radial_profile(data, dtheta, center, angles, phi):
+    lib = load()
+    d = np.ascontiguousarray(data, dtype=np.float64)
+    h, w = d.shape
+    a = np.ascontiguousarray(angles, dtype=np.float64)
+    out = np.empty(a.size, np.float64)
+    lib.ref_pattern_radial_profile(d.ctypes.data, w, h, float(dtheta), float(center[0]), float(center[1]),
+                                   a.ctypes.data, int(a.size), float(phi[0]), float(phi[1]), out.ctypes.data)
+    return out

@@ -818,3 +818,110 @@ def farfield_loss_grad(rho, S, A, loss="amplitude", eps=0.0):
     n0, n1 = rho.shape
     G = Sm * (np.fft.fft2(gF))  # unnormalised exponent -i: the adjoint of ft
     return L, G
+
+
+# ----------------------------------------------------------------------------
+# Detector-image preprocessing (src/pattern/pattern.cpp)
+# ----------------------------------------------------------------------------
+_WFRAC = 0.1
+
+
+def _splat(acc, wsum, ix, iy, val, nw, nh):
+    """Bilinear splat of values at fractional positions (pattern.cpp:36-74):
+    four neighbours, weights (1-dx)(1-dy) ... , out-of-range neighbours
+    dropped."""
+    ixt = np.floor(ix).astype(np.int64)
+    iyt = np.floor(iy).astype(np.int64)
+    xd, yd = ix - ixt, iy - iyt
+    for ox, oy, w in ((0, 0, (1 - xd) * (1 - yd)), (1, 0, xd * (1 - yd)), (0, 1, (1 - xd) * yd), (1, 1, xd * yd)):
+        x, y = ixt + ox, iyt + oy
+        ok = (x >= 0) & (y >= 0) & (x < nw) & (y < nh)
+        if acc is not None:
+            np.add.at(acc, y[ok] * nw + x[ok], (val * w)[ok])
+        np.add.at(wsum, y[ok] * nw + x[ok], w[ok])
+
+
+def _ewald(x, y, cx, cy, R, dx, dxn):
+    relx, rely = x - cx, y - cy
+    phi = np.arctan2(rely, relx)
+    theta = np.arctan2(np.sqrt(relx * relx + rely * rely) * dx, R)
+    rn = R * 2.0 * np.sin(theta / 2.0) / dxn
+    return rn * np.cos(phi), rn * np.sin(phi), theta
+
+
+def pattern_resample(mode, data, mask, center, R, dx, cutsize, newsize):
+    """Restates Pattern::downscale (mode 0, pattern.cpp:18-84),
+    downscale_and_correct (1, :88-186), cut_downscale_and_correct (2,
+    :190-317) and cut_and_downscale (3, :321-438).  Returns (data, mask)."""
+    d = np.asarray(data, dtype=np.float64)
+    h, w = d.shape
+    m = None if mask is None else np.asarray(mask, dtype=np.float64).reshape(h, w)
+    nw, nh = int(newsize[0]), int(newsize[1])
+    y, x = np.mgrid[0:h, 0:w]
+    x = x.ravel().astype(np.float64)
+    y = y.ravel().astype(np.float64)
+    dv = d.ravel()
+    mv = None if m is None else m.ravel()
+    od, tw = np.zeros(nw * nh), np.zeros(nw * nh)
+    om, mw = np.zeros(nw * nh), np.zeros(nw * nh)
+    cx, cy = float(center[0]), float(center[1])
+    cut = mode in (2, 3)
+    sf0 = (cutsize[0] if cut else w) / nw
+    sf1 = (cutsize[1] if cut else h) / nh
+    if mode in (1, 2):
+        maxdist = max(cx, cy, w - cx, h - cy)
+        dxn = R * 2.0 * math.sin(math.atan2(dx * maxdist, R) / 2.0) / maxdist
+    if mode == 0:
+        sel = dv >= 0
+        _splat(od, tw, x[sel] / sf0, y[sel] / sf0, dv[sel], nw, nh)
+        ref = tw
+    elif mode == 1:
+        sel = mv > 0.5
+        xn, yn, th = _ewald(x[sel], y[sel], cx, cy, R, dx, dxn)
+        _splat(od, tw, (xn + cx) / sf0, (yn + cy) / sf1, dv[sel] * (1.0 / np.cos(th) ** 3), nw, nh)
+        ref = np.full_like(tw, tw.max())
+    else:
+        if mode == 2:
+            xn, yn, th = _ewald(x, y, cx, cy, R, dx, dxn)
+            ix, iy = xn / sf0 + float(nw // 2), yn / sf1 + float(nh // 2)
+            val = dv * (1.0 / np.cos(th) ** 3)
+        else:
+            ix, iy = (x - cx) / sf0 + float(nw // 2), (y - cy) / sf1 + float(nh // 2)
+            val = dv
+        sel = mv > 0.5
+        _splat(od, tw, ix[sel], iy[sel], val[sel], nw, nh)
+        _splat(om, mw, ix, iy, mv, nw, nh)
+        ref = np.full_like(tw, tw.max()) if mode == 2 else mw
+    with np.errstate(divide="ignore", invalid="ignore"):
+        out = np.where(tw > _WFRAC * ref, od / np.where(tw > 0, tw, 1), -1.0)
+        outm = np.where(mw > _WFRAC * mw.max(), om / np.where(mw > 0, mw, 1), -1.0) if cut else None
+    return out.reshape(nh, nw), (None if outm is None else outm.reshape(nh, nw))
+
+
+def radial_profile(data, dtheta, center, angles, phi):
+    """Restates Pattern::get_radial_profile (pattern.cpp:450-512)."""
+    d = np.asarray(data, dtype=np.float64)
+    h, w = d.shape
+    ang = np.asarray(angles, dtype=np.float64)
+    y, x = np.mgrid[0:h, 0:w]
+    xr = x.ravel() - float(center[0])
+    yr = y.ravel() - float(center[1])
+    a = np.arctan2(yr, xr) / math.pi * 180.0
+    while True:
+        up = a + 360.0 <= phi[1]
+        if not up.any():
+            break
+        a = np.where(up, a + 360.0, a)
+    inside = (a <= phi[1]) & (a >= phi[0])
+    radius = np.sqrt(xr * xr + yr * yr) * dtheta
+    k = np.searchsorted(ang, radius, side="right") - 1
+    ok = inside & (k >= 0) & (k < ang.size - 1) & (d.ravel() >= 0)
+    k, r, v = k[ok], radius[ok], d.ravel()[ok]
+    f = (ang[k + 1] - r) / (ang[k + 1] - ang[k])
+    prof, norm = np.zeros(ang.size), np.zeros(ang.size)
+    np.add.at(prof, k, v * f)
+    np.add.at(norm, k, f)
+    np.add.at(prof, k + 1, v * (1 - f))
+    np.add.at(norm, k + 1, 1 - f)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(norm > 4, prof / np.where(norm > 0, norm, 1), -1.0)
