@@ -56,6 +56,7 @@ def parse():
                     help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
     ap.add_argument("--batch-patterns", type=int, default=256,
                     help="patterns of uneven sizes in the graph-captured batch (0: skip)")
+    ap.add_argument("--large", type=int, default=1, help="time the 2048^2 x 128 population (0: skip)")
     ap.add_argument("--refine", type=int, default=1, help="time the gradient-refinement epoch (0: skip)")
     ap.add_argument("--profile-loss", action="store_true", help="profiling case: one loss + gradient at 512^2 x 64")
     ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
@@ -376,6 +377,40 @@ def refinement(args, local):
             "rfactor_median": round(float(np.median([x["error_fourier"] for x in m])), 5)}
 
 
+def large_population(args, local):
+    """Large population: 2048 x 2048 complex64, 128 individuals (about 17 GB
+    of device state), starting population synthesised on the device
+    (spe_initialize_pop), RAAR beta 0.87; timed over 20 iterations."""
+    import torch
+    from s_spi_spring_gb300 import _lib, synthetic
+    n, P, iters = 2048, 128, 20
+    I, _, _ = synthetic.polygon_pattern(seed=9, n=n, diameter=480.0, photons=1e9, stop_radius=12, gap=6, stripes=3)
+    eng = _lib.Engine(n, local)
+    eng.set_amplitudes(_lib.prepare_pattern(I, (-1, -1), True))
+    eng.reserve(P)
+    eng.seed(42)
+    eng.initialize_pop(0, P, 600, (120.0, 540.0), (2, 8), (0.5, 0.5), (0.5, 1.5), 0.0)
+    eng.raar(0, P, 1, BETA, 0.0)
+    eng.synchronize()
+    st = torch.cuda.ExternalStream(eng.get_stream(), device=f"cuda:{local}") if eng.get_stream() else \
+        torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    eng.raar(0, P, iters, BETA, 0.0)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    m = eng.evaluate(0, P)
+    peak, kind = peaks()
+    alg = B_PER_PIXEL_ITER * n * n * P * iters
+    eng.close()
+    return {"workload": "2048x2048 complex64, 128 individuals, RAAR beta 0.87", "iterations": iters,
+            "ms_per_iteration": round(ms / iters, 3), "iter_ind_per_s": round(P * iters / (ms / 1e3), 1),
+            "alg_gbps": round(alg / (ms / 1e3) / 1e9, 1), "frac": round(alg / (ms / 1e3) / 1e9 / peak, 4),
+            "device_state_gb": round(P * n * n * 32 / 1e9, 1),
+            "rfactor_median": round(float(np.median([x["error_fourier"] for x in m])), 5)}
+
+
 def run_engine(args):
     import torch
     from s_spi_spring_gb300 import _lib
@@ -512,6 +547,11 @@ def run_engine(args):
             out["batched_sizes"] = batched_sizes(args, local)
         except Exception as ex:
             out["batched_sizes"] = {"error": str(ex)[:300]}
+    if rank == 0 and args.large:
+        try:
+            out["large_population"] = large_population(args, local)
+        except Exception as ex:
+            out["large_population"] = {"error": str(ex)[:300]}
     if rank == 0 and args.refine:
         try:
             out["refinement"] = refinement(args, local)

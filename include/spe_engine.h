@@ -222,6 +222,13 @@ int spe_initialize_pop(spe_engine* e, int first, int count, int support_size, fl
  * Overlapping source and destination ranges are rejected. */
 int spe_copy(spe_engine* e, int src, int dst, int count);
 
+/* |F| of individuals [first, first+count): the modulus of the iteration's
+ * transform (exponent +i, unnormalised), DC at [0,0], into the host array
+ * modulus (count*n*n floats).  The reconstructed pattern of the reference's
+ * Result::get_rec_pattern / get_prtf (spring/result.py:393-407, 688-717) is
+ * its square / itself after an fftshift. */
+int spe_far_field(spe_engine* e, int first, int count, float* modulus);
+
 /* Gathers individuals into a contiguous range: slot dst_first+k receives
  * slot src[k] (density and support), k < count, in one launch.  No source
  * slot may lie inside the destination range; a slot may be listed twice.

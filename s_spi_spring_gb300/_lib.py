@@ -78,6 +78,7 @@ SIGNATURES = {
     "spe_initialize_pop": (_i, [_vp, _i, _i, _i, _f, _f, _i, _i, _f, _f, _f, _f, _f, _f]),
     "spe_copy": (_i, [_vp, _i, _i, _i]),
     "spe_gather": (_i, [_vp, _ip, _i, _i]),
+    "spe_far_field": (_i, [_vp, _i, _i, _fp]),
     "spe_loss_grad": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp, _vp]),
     "spe_set_amplitudes_batch": (_i, [_vp, _fp, _i, _i]),
     "spe_adam_step": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _f, _f, _f, _f, _i, _vp]),
@@ -372,6 +373,12 @@ class Engine:
         d, s = self.device_buffers()
         off = int(first) * self.n * self.n
         return d + off * 8, s + off * 4
+
+    def far_field(self, first, count):
+        """|FFT+(rho)| of slots [first, first+count), DC at [0, 0]."""
+        out = np.empty((count, self.n, self.n), np.float32)
+        call("spe_far_field", self.h, int(first), int(count), fptr(out))
+        return out
 
     def gather(self, src_slots, dst_first):
         src = np.ascontiguousarray(src_slots, dtype=np.int32)

@@ -643,6 +643,23 @@ int spe_copy(spe_engine* e, int src, int dst, int count) {
   return SPE_OK;
 }
 
+int spe_far_field(spe_engine* e, int first, int count, float* modulus) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if (count == 0) return SPE_OK;
+  if (!modulus) return fail(SPE_ERR_INVALID, "null output");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  const size_t npix = e->npix;
+  if ((rc = ensure_work(e, (size_t)count * npix * (sizeof(float) + sizeof(float2)) + 512))) return rc;
+  Carve cv{(char*)e->work};
+  float* M = cv.take<float>((size_t)count * npix);
+  float2* tmp = cv.take<float2>((size_t)count * npix);
+  CK(e->ops->ft_magnitude(item_ctx(e, count, e->A), e->rho + (size_t)first * npix, tmp, M), "far-field transforms");
+  CK(cudaMemcpyAsync(modulus, M, (size_t)count * npix * sizeof(float), cudaMemcpyDeviceToHost, e->st), "download");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
+  return SPE_OK;
+}
+
 int spe_gather(spe_engine* e, const int* src, int count, int dst_first) {
   int rc = check_range(e, dst_first, count);
   if (rc) return rc;
