@@ -390,6 +390,8 @@ def large_population(args, local):
     eng.reserve(P)
     eng.seed(42)
     eng.initialize_pop(0, P, 600, (120.0, 540.0), (2, 8), (0.5, 0.5), (0.5, 1.5), 0.0)
+    tiles = eng.autotune(0, P, 2)
+    sched = eng.schedule()
     eng.raar(0, P, 1, BETA, 0.0)
     eng.synchronize()
     st = torch.cuda.ExternalStream(eng.get_stream(), device=f"cuda:{local}") if eng.get_stream() else \
@@ -407,7 +409,7 @@ def large_population(args, local):
     return {"workload": "2048x2048 complex64, 128 individuals, RAAR beta 0.87", "iterations": iters,
             "ms_per_iteration": round(ms / iters, 3), "iter_ind_per_s": round(P * iters / (ms / 1e3), 1),
             "alg_gbps": round(alg / (ms / 1e3) / 1e9, 1), "frac": round(alg / (ms / 1e3) / 1e9 / peak, 4),
-            "device_state_gb": round(P * n * n * 32 / 1e9, 1),
+            "device_state_gb": round(P * n * n * 32 / 1e9, 1), "tiles": list(tiles), "schedule": list(sched),
             "rfactor_median": round(float(np.median([x["error_fourier"] for x in m])), 5)}
 
 
@@ -427,7 +429,7 @@ def run_engine(args):
     stream = torch.cuda.Stream(device=local)
     eng.set_stream(stream.cuda_stream)
     eng.upload(0, dens, S)
-    tiles, sched = configure(eng, args, tune_iters=10)
+    tiles, sched = configure(eng, args, tune_iters=30)
     eng.synchronize()
 
     def barrier():

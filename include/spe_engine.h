@@ -349,8 +349,9 @@ int spe_get_schedule(spe_engine* e, int* chunk, int* lanes);
 /* Autotuner (no reference counterpart; the reference has fixed 32x32
  * blocks, gpu_context.h:17-21): times every compiled tile width of the
  * iteration kernels on the resident population [first, first+count) with
- * `iterations` RAAR steps per trial, then the schedule (spe_set_schedule,
- * blocks that fit in L2), keeps the fastest and restores the densities.
+ * `iterations` RAAR steps per trial -- the column width first, then row
+ * widths jointly with the schedule (spe_set_schedule) -- keeps the fastest
+ * and restores the densities.
  * cols / rows (may be NULL) receive the widths; spe_get_schedule the
  * schedule. */
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows);

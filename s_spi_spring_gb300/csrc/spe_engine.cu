@@ -255,12 +255,6 @@ spe::Ctx item_ctx(spe_engine* e, int count, const float* A) {
   return c;
 }
 
-size_t l2_bytes(int dev) {
-  int v = 0;
-  if (cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) != cudaSuccess || v <= 0) v = 64 << 20;
-  return (size_t)v;
-}
-
 // Runs `iters` iterations on [first, first+count) in blocks of `chunk`
 // individuals, each block through all its iterations before the next (the
 // individuals are independent, so the result equals one call on the whole
@@ -869,9 +863,9 @@ int spe_get_tiles(spe_engine* e, int* cols, int* rows) {
 
 // Times the compiled tile widths of the iteration kernels on the resident
 // population [first, first+count) (RAAR, `iterations` per trial, median of
-// three) -- first the column pass with the current row width, then the row
-// pass -- then the schedule (block size and lanes, blocks that fit in L2;
-// kept only when 2% faster than the whole range), keeps the fastest and
+// three) -- first the column pass with the current row width, then every row
+// width with every schedule (whole range, or blocks on one or two lanes; a
+// blocked schedule is kept only when 2% faster) -- keeps the fastest and
 // restores the densities.
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows) {
   int rc = check_range(e, first, count);
@@ -915,34 +909,32 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
       best_c = wcs[i];
     }
   }
-  best = 1e30f;
-  for (int i = 0; !rc && i < nr; ++i) {
-    float ms;
-    if ((rc = trial(best_c, wrs[i], &ms))) break;
-    if (ms < best) {
-      best = ms;
-      best_r = wrs[i];
-    }
-  }
-  // then the schedule: whole range, or L2-sized blocks on one or two lanes
+  // then row widths jointly with the schedule (the whole range, or blocks of
+  // individuals on one or two lanes: which one wins depends on the row width)
   int best_chunk = 0, best_lanes = 1;
-  if (!rc) {
-    float ms = 0.f;
-    rc = trial_s(best_c, best_r, 0, 1, &ms);
-    best = ms;
-    const size_t per_ind = e->npix * (2 * sizeof(float2) + sizeof(int));  // rho, T, S
-    const size_t l2 = l2_bytes(e->dev);
-    for (int lanes = 1; !rc && lanes <= 2; ++lanes)
-      for (int chunk : {32, 24, 16, 12, 8, 4}) {
-        if (chunk >= count || (size_t)chunk * lanes * per_ind > l2) continue;
-        if ((rc = trial_s(best_c, best_r, chunk, lanes, &ms))) break;
-        if (ms < best * 0.98f) {
-          best = ms;
-          best_chunk = chunk;
-          best_lanes = lanes;
-        }
+  best = 1e30f;
+  int sched[16][2];
+  int ns = 0;
+  sched[ns][0] = 0, sched[ns][1] = 1, ++ns;
+  for (int lanes = 1; lanes <= 2; ++lanes)
+    for (int chunk : {count / 2, 32, 24, 16, 8}) {
+      bool dup = chunk <= 0 || chunk >= count;
+      for (int k = 0; k < ns && !dup; ++k) dup = sched[k][0] == chunk && sched[k][1] == lanes;
+      if (!dup && ns < 16) sched[ns][0] = chunk, sched[ns][1] = lanes, ++ns;
+    }
+  for (int i = 0; !rc && i < nr; ++i)
+    for (int k = 0; !rc && k < ns; ++k) {
+      float ms;
+      if ((rc = trial_s(best_c, wrs[i], sched[k][0], sched[k][1], &ms))) break;
+      // a schedule other than the whole range must win by 2%
+      const float bar = (sched[k][0] == 0) ? best : best * 0.98f;
+      if (ms < bar) {
+        best = ms;
+        best_r = wrs[i];
+        best_chunk = sched[k][0];
+        best_lanes = sched[k][1];
       }
-  }
+    }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;

@@ -167,6 +167,13 @@ def test_converged_rfactor_matches_oracle(alg, beta):
         ref = o.get_error(r, S[i], A, 0.0).error_fourier
         print(alg, i, ms[i]["error_fourier"], ref)
         assert abs(ms[i]["error_fourier"] - ref) < 1e-4
+        # the final reconstruction, after translation / global-phase / twin
+        # alignment to the oracle's (a13 semantics), agrees within 1e-3
+        got = e.download(i, 1)[0][0].astype(complex)
+        aligned, _ = o.reshift(got, S[i], r, A)
+        err = np.linalg.norm(aligned - r) / np.linalg.norm(r)
+        print(alg, i, "aligned reconstruction error", err)
+        assert err < 1e-3
 
 
 def test_subset_range_leaves_others_untouched():
