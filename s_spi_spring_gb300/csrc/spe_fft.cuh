@@ -272,10 +272,23 @@ void fill_twiddles(float2* out) {
 // barrier between the exchange stores and loads: the whole CTA, or (when
 // every sequence lives inside one warp) the warp
 struct SyncCTA {
-  static __device__ __forceinline__ void sync() { __syncthreads(); }
+  static __device__ __forceinline__ void sync(int) { __syncthreads(); }
 };
 struct SyncWarp {
-  static __device__ __forceinline__ void sync() { __syncwarp(); }
+  static __device__ __forceinline__ void sync(int) { __syncwarp(); }
+};
+// the TPT threads of sequence c only (consecutive threads; TPT a multiple of
+// 32 uses hardware barrier 1 + c, which must stay below 16)
+template <int TPT>
+struct SyncGroup {
+  static __device__ __forceinline__ void sync(int c) {
+    if constexpr (TPT <= 32) {
+      __syncwarp();
+    } else {
+      static_assert(TPT % 32 == 0, "a barrier group is whole warps");
+      asm volatile("bar.sync %0, %1;" ::"r"(1 + c), "r"(TPT) : "memory");
+    }
+  }
 };
 
 template <int L, int TPT, int S, class Lay, int P, int NS, class Sync = SyncCTA>
@@ -311,7 +324,7 @@ __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf
 #pragma unroll
       for (int q = 0; q < R; ++q) buf[Lay::idx(base + q * NS, c)] = v[u * R + q];
     }
-    Sync::sync();
+    Sync::sync(c);
     constexpr int R2 = Rad::value[P + 1];
     constexpr int NB2 = L / R2;
     constexpr int U2 = NB2 / TPT;
@@ -322,7 +335,7 @@ __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf
 #pragma unroll
       for (int r = 0; r < R2; ++r) v[u * R2 + r] = buf[Lay::idx(b + r * NB2, c)];
     }
-    Sync::sync();
+    Sync::sync(c);
     fft_pass_reg<L, TPT, S, Lay, P + 1, NS * R, Sync>(v, buf, tw, c, j);
   }
 }

@@ -517,9 +517,9 @@ struct LayColMajor {
   static __device__ __forceinline__ int idx(int l, int c) { return c * CS + l + (l >> 4); }
 };
 
-template <int N, int W>
+template <int N, int W, int TPT_ = 32>
 struct WarpCfg {
-  static constexpr int TPT = 32;
+  static constexpr int TPT = TPT_;
   static constexpr int E = N / TPT;
   static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
   static constexpr int NT = W * TPT;
@@ -528,15 +528,19 @@ struct WarpCfg {
   static constexpr int C_A = align128(W * ACS * 4);
   static constexpr int STAGE = C_T + C_A;
   static constexpr size_t SMEM = (size_t)TWB + 2 * STAGE;
-  static constexpr int MINB_RAW = 65536 / (NT * 128);
+  static constexpr int MINB_RAW = 65536 / (NT * (E <= 8 ? 64 : 128));
   static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
 };
 
-template <int N, int W>
-__global__ void __launch_bounds__(WarpCfg<N, W>::NT, WarpCfg<N, W>::MINB)
+// TPT consecutive threads per column: TPT = 32 keeps a column in one warp
+// (warp-synchronous exchanges); larger TPT meets at the column's own
+// hardware barrier
+template <int N, int W, int TPT>
+__global__ void __launch_bounds__(WarpCfg<N, W, TPT>::NT, WarpCfg<N, W, TPT>::MINB)
     k_cols_warp(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count,
                 const float2* __restrict__ twg) {
-  using C = WarpCfg<N, W>;
+  using C = WarpCfg<N, W, TPT>;
+  using Sync = SyncGroup<TPT>;
   constexpr int NT = C::NT, E = C::E, TPI = N / W, ACS = C::ACS;
   using Lay = LayColMajor<N, W>;
   extern __shared__ __align__(128) unsigned char sm[];
@@ -546,7 +550,7 @@ __global__ void __launch_bounds__(WarpCfg<N, W>::NT, WarpCfg<N, W>::MINB)
   load_twiddles<N>(tw, twg, NT);
   pdl_wait();
   const int t = threadIdx.x;
-  const int c = t >> 5, j = t & 31;
+  const int c = t / TPT, j = t % TPT;
   const int ntiles = count * TPI;
 
   auto stage_tile = [&](int tile, int s) {
@@ -579,14 +583,14 @@ __global__ void __launch_bounds__(WarpCfg<N, W>::NT, WarpCfg<N, W>::MINB)
     const int x0 = (tile % TPI) * W;
     float2 v[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = sT[Lay::idx(elem_pos_t<N, 32>(e, j), c)];
-    __syncwarp();  // column c's region becomes this warp's exchange buffer
-    fft_pass_reg<N, 32, +1, Lay, 0, 1, SyncWarp>(v, sT, tw, c, j);
+    for (int e = 0; e < E; ++e) v[e] = sT[Lay::idx(elem_pos_t<N, TPT>(e, j), c)];
+    Sync::sync(c);  // column c's region becomes its exchange buffer
+    fft_pass_reg<N, TPT, +1, Lay, 0, 1, Sync>(v, sT, tw, c, j);
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = project(v[e], sA[c * ACS + elem_pos_t<N, 32>(e, j)]);
-    fft_pass_reg<N, 32, -1, Lay, 0, 1, SyncWarp>(v, sT, tw, c, j);
+    for (int e = 0; e < E; ++e) v[e] = project(v[e], sA[c * ACS + elem_pos_t<N, TPT>(e, j)]);
+    fft_pass_reg<N, TPT, -1, Lay, 0, 1, Sync>(v, sT, tw, c, j);
 #pragma unroll
-    for (int e = 0; e < E; ++e) sT[Lay::idx(elem_pos_t<N, 32>(e, j), c)] = v[e];
+    for (int e = 0; e < E; ++e) sT[Lay::idx(elem_pos_t<N, TPT>(e, j), c)] = v[e];
     __syncthreads();  // every column of the tile is in shared memory
     float2* gT = T + (size_t)p * N * N + x0;
     for (int q = t; q < N * W / 2; q += NT) {

@@ -77,19 +77,29 @@ constexpr bool pair_ok() {
   return W % 4 == 0 && W <= N && N % W == 0 && Elems<N>::value <= 8 && PairCfg<N, W / 2>::NT % 32 == 0 &&
          PairCfg<N, W / 2>::NT <= 1024 && PairCfg<N, W / 2>::SMEM <= kMaxSmem;
 }
-// one-warp-per-column variants: every pass's butterflies divide over 32
-// threads with at most 16 elements per thread
-template <int N>
-constexpr bool warp_plan_ok() {
+// column-major variants (TPT consecutive threads per column): every pass's
+// butterflies divide over TPT threads, at most 16 elements per thread, and
+// with barrier groups (TPT > 32) at most 15 columns per tile
+template <int N, int TPT>
+constexpr bool cm_plan_ok() {
   using Rad = typename Plan<N>::R;
   for (int p = 0; p < Rad::count; ++p)
-    if ((N / Rad::value[p]) % 32 != 0) return false;
-  return N / 32 <= 16;
+    if ((N / Rad::value[p]) % TPT != 0) return false;
+  return N / TPT <= 16;
+}
+template <int N, int W, int TPT>
+constexpr bool cm_ok() {
+  return cm_plan_ok<N, TPT>() && W <= N && N % W == 0 && W % 2 == 0 && (TPT <= 32 || W <= 15) &&
+         WarpCfg<N, W, TPT>::NT <= 1024 && WarpCfg<N, W, TPT>::SMEM <= kMaxSmem;
 }
 template <int N, int W>
 constexpr bool warpcol_ok() {
-  return warp_plan_ok<N>() && W <= N && N % W == 0 && W % 2 == 0 && WarpCfg<N, W>::NT <= 1024 &&
-         WarpCfg<N, W>::SMEM <= kMaxSmem;
+  return cm_ok<N, W, 32>();
+}
+// the plan's own threads per column, when that is more than a warp
+template <int N, int W>
+constexpr bool groupcol_ok() {
+  return Plan<N>::TPT > 32 && cm_ok<N, W, Plan<N>::TPT>();
 }
 constexpr int kColWidths[3] = {4, 8, 16};
 constexpr int kRowWidths[5] = {1, 2, 4, 8, 16};
@@ -183,10 +193,10 @@ cudaError_t launch_cols_pair(const Ctx& c) {
   return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, c.tw);
 }
 
-template <int N, int W>
+template <int N, int W, int TPT>
 cudaError_t launch_cols_warp(const Ctx& c) {
-  using P = WarpCfg<N, W>;
-  auto kern = k_cols_warp<N, W>;
+  using P = WarpCfg<N, W, TPT>;
+  auto kern = k_cols_warp<N, W, TPT>;
   static unsigned long long configured = 0ull;
   static int resident[64] = {0};
   cudaError_t e = configure(kern, P::SMEM, configured);
@@ -213,13 +223,16 @@ cudaError_t launch_cols_loss(const Ctx& c, float eps, double* partials) {
 
 // column-pass variant code: W > 0 one column per thread, W columns per tile;
 // W < 0 two columns per thread, -W columns per tile; 100 + W one warp per
-// column, W columns per tile
+// column, 200 + W the plan's threads per column (column-major tile, barrier
+// per column), W columns per tile
 template <int N>
 cudaError_t launch_cols_w(const Ctx& c, int w) {
   switch (w) {
-    case 104: if constexpr (warpcol_ok<N, 4>()) return launch_cols_warp<N, 4>(c); break;
-    case 108: if constexpr (warpcol_ok<N, 8>()) return launch_cols_warp<N, 8>(c); break;
-    case 116: if constexpr (warpcol_ok<N, 16>()) return launch_cols_warp<N, 16>(c); break;
+    case 104: if constexpr (warpcol_ok<N, 4>()) return launch_cols_warp<N, 4, 32>(c); break;
+    case 108: if constexpr (warpcol_ok<N, 8>()) return launch_cols_warp<N, 8, 32>(c); break;
+    case 116: if constexpr (warpcol_ok<N, 16>()) return launch_cols_warp<N, 16, 32>(c); break;
+    case 204: if constexpr (groupcol_ok<N, 4>()) return launch_cols_warp<N, 4, Plan<N>::TPT>(c); break;
+    case 208: if constexpr (groupcol_ok<N, 8>()) return launch_cols_warp<N, 8, Plan<N>::TPT>(c); break;
     case -4: if constexpr (pair_ok<N, 4>()) return launch_cols_pair<N, 4>(c); break;
     case -8: if constexpr (pair_ok<N, 8>()) return launch_cols_pair<N, 8>(c); break;
     case -16: if constexpr (pair_ok<N, 16>()) return launch_cols_pair<N, 16>(c); break;
@@ -322,6 +335,8 @@ struct SizeImpl {
     if constexpr (warpcol_ok<N, 4>()) out[k++] = 104;
     if constexpr (warpcol_ok<N, 8>()) out[k++] = 108;
     if constexpr (warpcol_ok<N, 16>()) out[k++] = 116;
+    if constexpr (groupcol_ok<N, 4>()) out[k++] = 204;
+    if constexpr (groupcol_ok<N, 8>()) out[k++] = 208;
     if constexpr (pair_ok<N, 4>()) out[k++] = -4;
     if constexpr (pair_ok<N, 8>()) out[k++] = -8;
     if constexpr (pair_ok<N, 16>()) out[k++] = -16;
