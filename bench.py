@@ -650,8 +650,11 @@ def run_profile_loss():
     for _ in range(2):
         x = d.detach().requires_grad_(True)
         FarFieldLoss.apply(x, s, eng, "poisson", 1e-6).sum().backward()
+    # and two fused refinement steps (loss, adjoint, Adam update)
+    from s_spi_spring_gb300.refine import refine
+    refine(eng, 0, POP, steps=2, lr=1e-4, loss="poisson", eps=1e-6, fused=True)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_case": "loss+gradient", "n": N, "population": POP}))
+    print(json.dumps({"profile_case": "loss+gradient, fused Adam steps", "n": N, "population": POP}))
 
 
 def run_profile_case(args):

@@ -268,7 +268,8 @@ int spe_get_tiles(spe_engine* e, int* cols, int* rows);
  * NULL for 1): support * FFT-(2 dL/dconj F), the gradient convention of
  * complex autograd.  The transform is recomputed, nothing is stored between
  * the loss and the gradient.  Runs on the engine's stream; the engine's
- * population capacity grows to `count` for scratch. */
+ * population capacity grows to `count` for scratch, so arrays that alias the
+ * engine's own slots (spe_device_buffers) need count <= spe_capacity. */
 enum { SPE_LOSS_AMPLITUDE = 0, SPE_LOSS_POISSON = 1 };
 int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
                   double* loss_out, void* grad_out, const float* grad_scale);
@@ -300,7 +301,8 @@ int spe_graph_destroy(spe_graph* g);
  * reals) applied in place to `density`, with the first and second moments
  * in exp_avg / exp_avg_sq (device, complex64 layout, count*n*n each, zero
  * before step 1).  `step` counts from 1.  The gradient never reaches memory:
- * the last pass of the adjoint applies the update. */
+ * the last pass of the adjoint applies the update.  As for spe_loss_grad,
+ * arrays aliasing the engine's slots need count <= spe_capacity. */
 int spe_adam_step(spe_engine* e, void* density, const int32_t* support, void* exp_avg, void* exp_avg_sq, int count,
                   int loss, float eps, float lr, float beta1, float beta2, float adam_eps, int step,
                   double* loss_out);
