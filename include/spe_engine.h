@@ -140,6 +140,19 @@ int spe_hio(spe_engine* e, int first, int count, int iterations, float beta, flo
 int spe_raar(spe_engine* e, int first, int count, int iterations, float beta, float reality);
 int spe_er(spe_engine* e, int first, int count, int iterations, float reality);
 
+/* Solver::HIO / RAAR / ER as the reference's host interface uses them
+ * (src/solver.cpp:360-411: densities in host memory, results back in host
+ * memory): `count` individuals from the host arrays density (complex64) and
+ * support (int32; NULL keeps the resident supports) go to slots
+ * [first, first+count), run `iterations` of `algorithm` (SPE_OP_HIO / RAAR /
+ * ER), and come back into density_out (may be `density`).  The population
+ * is split into `blocks` blocks (<= 0: 2) on two streams, so one block's
+ * copies overlap another's iterations; with page-locked host buffers the
+ * copies are asynchronous.  Returns when density_out is complete.  Results
+ * equal spe_upload + spe_hio/raar/er + spe_download. */
+int spe_iterate_host(spe_engine* e, int first, int count, const float* density, const int32_t* support,
+                     int algorithm, int iterations, float beta, float reality, float* density_out, int blocks);
+
 /* Shrink-wrap support updates: GPU_context::SW / SWA
  * (gpu_context.cu:906-1027), Solver::SW / SWA (src/solver.cpp:414-450).
  * SW keeps pixels whose blurred modulus is >= threshold * max; SWA keeps the

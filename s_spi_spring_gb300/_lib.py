@@ -78,6 +78,7 @@ SIGNATURES = {
     "spe_initialize_pop": (_i, [_vp, _i, _i, _i, _f, _f, _i, _i, _f, _f, _f, _f, _f, _f]),
     "spe_copy": (_i, [_vp, _i, _i, _i]),
     "spe_gather": (_i, [_vp, _ip, _i, _i]),
+    "spe_iterate_host": (_i, [_vp, _i, _i, _fp, _ip, _i, _i, _f, _f, _fp, _i]),
     "spe_far_field": (_i, [_vp, _i, _i, _fp]),
     "spe_loss_grad": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp, _vp]),
     "spe_set_amplitudes_batch": (_i, [_vp, _fp, _i, _i]),
@@ -373,6 +374,19 @@ class Engine:
         d, s = self.device_buffers()
         off = int(first) * self.n * self.n
         return d + off * 8, s + off * 4
+
+    def iterate_host(self, first, density, support, algorithm, iterations, beta=0.0, reality=0.0, out=None,
+                     blocks=0):
+        """Host arrays in, iterations, host array out (copies overlapped with
+        the iterations of other blocks); returns the densities."""
+        d = np.ascontiguousarray(density, dtype=np.complex64)
+        s = None if support is None else np.ascontiguousarray(support, dtype=np.int32)
+        count = d.size // (self.n * self.n)
+        out = np.empty_like(d) if out is None else out
+        call("spe_iterate_host", self.h, int(first), int(count), d.view(np.float32).ctypes.data_as(_fp), iptr(s),
+             int(algorithm), int(iterations), float(beta), float(reality), out.view(np.float32).ctypes.data_as(_fp),
+             int(blocks))
+        return out
 
     def far_field(self, first, count):
         """|FFT+(rho)| of slots [first, first+count), DC at [0, 0]."""

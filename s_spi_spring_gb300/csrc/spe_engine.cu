@@ -255,6 +255,17 @@ spe::Ctx item_ctx(spe_engine* e, int count, const float* A) {
   return c;
 }
 
+// the second stream and its events (created on first use)
+int ensure_lanes(spe_engine* e) {
+  if (!e->lane2) {
+    CK(cudaStreamCreateWithFlags(&e->lane2, cudaStreamNonBlocking), "lane stream");
+    CK(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming), "lane event");
+    CK(cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming), "lane event");
+    CK(cudaEventCreateWithFlags(&e->phase, cudaEventDisableTiming), "lane event");
+  }
+  return SPE_OK;
+}
+
 // Runs `iters` iterations on [first, first+count) in blocks of `chunk`
 // individuals, each block through all its iterations before the next (the
 // individuals are independent, so the result equals one call on the whole
@@ -272,12 +283,8 @@ int run_iterations(spe_engine* e, int first, int count, int upd, int iters, floa
     }
     return SPE_OK;
   }
-  if (!e->lane2) {
-    CK(cudaStreamCreateWithFlags(&e->lane2, cudaStreamNonBlocking), "lane stream");
-    CK(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming), "lane event");
-    CK(cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming), "lane event");
-    CK(cudaEventCreateWithFlags(&e->phase, cudaEventDisableTiming), "lane event");
-  }
+  int rc = ensure_lanes(e);
+  if (rc) return rc;
   CK(cudaEventRecord(e->fork, e->st), "fork");
   CK(cudaStreamWaitEvent(e->lane2, e->fork, 0), "fork");
   for (int b = 0; b < nblocks; ++b) {
@@ -613,6 +620,53 @@ int spe_device_buffers(spe_engine* e, void** density, void** support) {
   if (!e) return fail(SPE_ERR_INVALID, "null engine");
   if (density) *density = e->rho;
   if (support) *support = e->S;
+  return SPE_OK;
+}
+
+int spe_iterate_host(spe_engine* e, int first, int count, const float* density, const int32_t* support,
+                     int algorithm, int iterations, float beta, float reality, float* density_out, int blocks) {
+  int rc = check_range(e, first, count);
+  if (rc) return rc;
+  if ((rc = need_amp(e))) return rc;
+  if ((rc = have_patterns(e, first, count))) return rc;
+  if (algorithm != SPE_OP_HIO && algorithm != SPE_OP_RAAR && algorithm != SPE_OP_ER)
+    return fail(SPE_ERR_INVALID, "algorithm must be SPE_OP_HIO, SPE_OP_RAAR or SPE_OP_ER");
+  if (iterations < 0) return fail(SPE_ERR_INVALID, "negative iteration count");
+  if (count == 0) return SPE_OK;
+  if (!density || !density_out) return fail(SPE_ERR_INVALID, "null host density");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  if ((rc = ensure_lanes(e))) return rc;
+  const int upd = (algorithm == SPE_OP_HIO) ? 0 : (algorithm == SPE_OP_RAAR ? 1 : 2);
+  const spe::Gate g = (upd == 1) ? gate_raar(reality) : gate_er(reality);
+  if (blocks <= 0) blocks = 2;
+  if (blocks > count) blocks = count;
+  const int chunk = (count + blocks - 1) / blocks;
+  const int nblocks = (count + chunk - 1) / chunk;
+  const size_t np = e->npix;
+  CK(cudaEventRecord(e->fork, e->st), "fork");
+  CK(cudaStreamWaitEvent(e->lane2, e->fork, 0), "fork");
+  for (int b = 0; b < nblocks; ++b) {
+    const int f = first + b * chunk, k = std::min(chunk, first + count - f);
+    const size_t h = (size_t)(f - first) * np;  // offset in the host arrays
+    cudaStream_t st = (b & 1) ? e->lane2 : e->st;
+    CK(cudaMemcpyAsync(e->rho + (size_t)f * np, reinterpret_cast<const float2*>(density) + h,
+                       (size_t)k * np * sizeof(float2), cudaMemcpyHostToDevice, st),
+       "upload density");
+    if (support)
+      CK(cudaMemcpyAsync(e->S + (size_t)f * np, support + h, (size_t)k * np * sizeof(int), cudaMemcpyHostToDevice,
+                         st),
+         "upload support");
+    spe::Ctx c = make_ctx(e, f, k);
+    c.st = st;
+    c.grid_div = nblocks > 1 ? 2 : 1;
+    CK(e->ops->iterate(c, upd, iterations, beta, g, e->tile_cols, e->tile_rows), "iteration kernels");
+    CK(cudaMemcpyAsync(reinterpret_cast<float2*>(density_out) + h, e->rho + (size_t)f * np,
+                       (size_t)k * np * sizeof(float2), cudaMemcpyDeviceToHost, st),
+       "download density");
+  }
+  CK(cudaEventRecord(e->join, e->lane2), "join");
+  CK(cudaStreamWaitEvent(e->st, e->join, 0), "join");
+  CK(cudaStreamSynchronize(e->st), "synchronize");
   return SPE_OK;
 }
 

@@ -70,6 +70,8 @@ size_t region(spe_engine* e);
 int reduce(spe_engine* e, const double* part, int count, int tpi, int k, int is_max, int slot);
 int reduce_peak(spe_engine* e, const double* part, int count, int slot);
 int fetch_red(spe_engine* e, int count);
+int ensure_lanes(spe_engine* e);
+int have_patterns(spe_engine* e, int first, int count);
 int run_iterations(spe_engine* e, int first, int count, int upd, int iters, float beta, const spe::Gate& g, int chunk,
                    int lanes, int wc, int wr);
 }  // namespace spe_detail

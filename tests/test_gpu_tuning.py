@@ -91,3 +91,20 @@ def test_autotune_schedule_is_valid():
     assert lanes in (1, 2) and 0 <= chunk < P
     got, _ = e.download(0, P)
     assert np.array_equal(got, dens)
+
+
+@pytest.mark.parametrize("blocks", [0, 1, 3, 7])
+def test_iterate_host_equals_upload_iterate_download(blocks):
+    """The pipelined host-buffer call gives the same results as separate
+    upload, iteration and download calls."""
+    n, P = 256, 7
+    e, dens, S = engine(n, P, seed=3)
+    e.upload(0, dens, S)
+    e.raar(0, P, 5, 0.87, 0.0)
+    ref, _ = e.download(0, P)
+    got = e.iterate_host(0, dens, S, _lib.SPE_OP_RAAR, 5, 0.87, 0.0, blocks=blocks)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    # in place, resident supports kept
+    buf = dens.copy()
+    e.iterate_host(0, buf, None, _lib.SPE_OP_RAAR, 5, 0.87, 0.0, out=buf, blocks=blocks)
+    assert np.array_equal(buf.view(np.uint32), ref.view(np.uint32))
