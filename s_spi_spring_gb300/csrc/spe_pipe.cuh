@@ -45,15 +45,24 @@ struct LayCol {
   }
 };
 
+// Alternative column layout: one padding row after every 8, so that every
+// exchange address is the thread's base plus a compile-time offset (no
+// per-access swizzle arithmetic).
+template <int L, int W>
+struct LayColPad {
+  static constexpr int SIZE = (L + L / 8) * W;
+  static __device__ __forceinline__ int idx(int l, int c) { return (l + (l >> 3)) * W + c; }
+};
+
 constexpr int align128(int b) { return (b + 127) & ~127; }
 
-template <int N, int W>
+template <int N, int W, class Lay = LayCol<N, W>>
 struct ColCfg {  // column pass with W columns per tile
   static constexpr int TPT = Plan<N>::TPT;
   static constexpr int E = Elems<N>::value;
   static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
   static constexpr int NT = W * TPT;
-  static constexpr int C_T = align128(LayCol<N, W>::SIZE * 8);
+  static constexpr int C_T = align128(Lay::SIZE * 8);
   static constexpr int C_A = align128(N * W * 4);
   static constexpr int STAGE = C_T + C_A;
   static constexpr size_t SMEM = (size_t)TWB + 2 * STAGE;
@@ -99,13 +108,13 @@ __device__ __forceinline__ void pdl_enter() {
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // column pass: T -> FFT+ (y) -> P_M with A -> FFT- (y) -> T
-template <int N, int W>
-__global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
+template <int N, int W, class LayT = LayCol<N, W>>
+__global__ void __launch_bounds__(ColCfg<N, W, LayT>::NT, ColCfg<N, W, LayT>::MINB)
     k_cols_project(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count,
                    const float2* __restrict__ twg) {
-  using C = ColCfg<N, W>;
+  using C = ColCfg<N, W, LayT>;
   constexpr int NT = C::NT, E = C::E, TPI = N / W;
-  using Lay = LayCol<N, W>;
+  using Lay = LayT;
   extern __shared__ __align__(128) unsigned char sm[];
   float2* tw = reinterpret_cast<float2*>(sm);
   unsigned char* stages = sm + C::TWB;

@@ -96,6 +96,11 @@ template <int N, int W>
 constexpr bool warpcol_ok() {
   return cm_ok<N, W, 32>();
 }
+// the column pass with the padded (affine) exchange layout
+template <int N, int W>
+constexpr bool padcol_ok() {
+  return col_ok<N, W>() && ColCfg<N, W, LayColPad<N, W>>::SMEM <= kMaxSmem;
+}
 // the plan's own threads per column, when that is more than a warp
 template <int N, int W>
 constexpr bool groupcol_ok() {
@@ -150,10 +155,10 @@ inline int share(int slots, int div) {
   return s < 1 ? 1 : s;
 }
 
-template <int N, int W>
+template <int N, int W, class Lay = LayCol<N, W>>
 cudaError_t launch_cols_project(const Ctx& c) {
-  using P = ColCfg<N, W>;
-  auto kern = k_cols_project<N, W>;
+  using P = ColCfg<N, W, Lay>;
+  auto kern = k_cols_project<N, W, Lay>;
   static unsigned long long configured = 0ull;
   static int resident[64] = {0};
   cudaError_t e = configure(kern, P::SMEM, configured);
@@ -224,13 +229,16 @@ cudaError_t launch_cols_loss(const Ctx& c, float eps, double* partials) {
 // column-pass variant code: W > 0 one column per thread, W columns per tile;
 // W < 0 two columns per thread, -W columns per tile; 100 + W one warp per
 // column, 200 + W the plan's threads per column (column-major tile, barrier
-// per column), W columns per tile
+// per column), 300 + W one column per thread with the padded layout, W
+// columns per tile
 template <int N>
 cudaError_t launch_cols_w(const Ctx& c, int w) {
   switch (w) {
     case 104: if constexpr (warpcol_ok<N, 4>()) return launch_cols_warp<N, 4, 32>(c); break;
     case 108: if constexpr (warpcol_ok<N, 8>()) return launch_cols_warp<N, 8, 32>(c); break;
     case 116: if constexpr (warpcol_ok<N, 16>()) return launch_cols_warp<N, 16, 32>(c); break;
+    case 304: if constexpr (padcol_ok<N, 4>()) return launch_cols_project<N, 4, LayColPad<N, 4>>(c); break;
+    case 308: if constexpr (padcol_ok<N, 8>()) return launch_cols_project<N, 8, LayColPad<N, 8>>(c); break;
     case 204: if constexpr (groupcol_ok<N, 4>()) return launch_cols_warp<N, 4, Plan<N>::TPT>(c); break;
     case 208: if constexpr (groupcol_ok<N, 8>()) return launch_cols_warp<N, 8, Plan<N>::TPT>(c); break;
     case -4: if constexpr (pair_ok<N, 4>()) return launch_cols_pair<N, 4>(c); break;
@@ -335,6 +343,8 @@ struct SizeImpl {
     if constexpr (warpcol_ok<N, 4>()) out[k++] = 104;
     if constexpr (warpcol_ok<N, 8>()) out[k++] = 108;
     if constexpr (warpcol_ok<N, 16>()) out[k++] = 116;
+    if constexpr (padcol_ok<N, 4>()) out[k++] = 304;
+    if constexpr (padcol_ok<N, 8>()) out[k++] = 308;
     if constexpr (groupcol_ok<N, 4>()) out[k++] = 204;
     if constexpr (groupcol_ok<N, 8>()) out[k++] = 208;
     if constexpr (pair_ok<N, 4>()) out[k++] = -4;
