@@ -32,6 +32,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace spe {
 
 // ---------------------------------------------------------------------------
@@ -196,6 +198,22 @@ struct LayPad {  // row passes
   static constexpr int STRIDE = L + L / 16;
   static constexpr int SIZE = W * STRIDE;
   static __device__ __forceinline__ int idx(int l, int c) { return c * STRIDE + l + (l >> 4); }
+  // split addressing (see store_addr / load_addr below): steps that are
+  // multiples of 16 add step + step/16; the radix-8 stores of the first two
+  // passes add q, and 8q + q/2
+  static constexpr bool kFastAddr = true;
+  template <int STEP>
+  static __device__ __forceinline__ int load_addr(int b, int r, int c) {
+    if constexpr (STEP % 16 == 0) return idx(b, c) + r * (STEP + STEP / 16);
+    else return idx(b + r * STEP, c);
+  }
+  template <int NS, int R>
+  static __device__ __forceinline__ int store_addr(int base, int q, int c) {
+    if constexpr (NS % 16 == 0) return idx(base, c) + q * (NS + NS / 16);
+    else if constexpr (NS == 1 && R == 8) return idx(base, c) + q;                 // base = 8b
+    else if constexpr (NS == 8 && R == 8) return idx(base, c) + 8 * q + (q >> 1);  // base = 64(b/8) + b%8
+    else return idx(base + q * NS, c);
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -291,6 +309,28 @@ struct SyncGroup {
   }
 };
 
+// Exchange addressing.  A layout may split the address of a Stockham store
+// (position base + q*NS) or load (position b + r*STEP) into a per-thread
+// part and a compile-time offset (store_addr / load_addr, announced by
+// kFastAddr); the compiler then forms one base per butterfly instead of
+// evaluating the layout function for every element.  Otherwise idx() is
+// used element by element.
+template <class Lay, class = void>
+struct HasFastAddr : std::false_type {};
+template <class Lay>
+struct HasFastAddr<Lay, std::void_t<decltype(Lay::kFastAddr)>> : std::true_type {};
+
+template <class Lay, int NS, int R>
+__device__ __forceinline__ int store_addr(int base, int q, int c) {
+  if constexpr (HasFastAddr<Lay>::value) return Lay::template store_addr<NS, R>(base, q, c);
+  else return Lay::idx(base + q * NS, c);
+}
+template <class Lay, int STEP>
+__device__ __forceinline__ int load_addr(int b, int r, int c) {
+  if constexpr (HasFastAddr<Lay>::value) return Lay::template load_addr<STEP>(b, r, c);
+  else return Lay::idx(b + r * STEP, c);
+}
+
 template <int L, int TPT, int S, class Lay, int P, int NS, class Sync = SyncCTA>
 __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf, const float2* __restrict__ tw,
                                              int c, int j) {
@@ -322,7 +362,7 @@ __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf
       const int k = (NS == 1) ? 0 : (b % NS);
       const int base = (b / NS) * NS * R + k;
 #pragma unroll
-      for (int q = 0; q < R; ++q) buf[Lay::idx(base + q * NS, c)] = v[u * R + q];
+      for (int q = 0; q < R; ++q) buf[store_addr<Lay, NS, R>(base, q, c)] = v[u * R + q];
     }
     Sync::sync(c);
     constexpr int R2 = Rad::value[P + 1];
@@ -333,7 +373,7 @@ __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf
     for (int u = 0; u < U2; ++u) {
       const int b = j + TPT * u;
 #pragma unroll
-      for (int r = 0; r < R2; ++r) v[u * R2 + r] = buf[Lay::idx(b + r * NB2, c)];
+      for (int r = 0; r < R2; ++r) v[u * R2 + r] = buf[load_addr<Lay, NB2>(b, r, c)];
     }
     Sync::sync(c);
     fft_pass_reg<L, TPT, S, Lay, P + 1, NS * R, Sync>(v, buf, tw, c, j);

@@ -39,9 +39,35 @@ __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wa
 template <int L, int W>
 struct LayCol {
   static constexpr int SIZE = L * W;
+  static constexpr int M = (W >= 16) ? 0 : 16 / W - 1;  // row swizzle mask
   static __device__ __forceinline__ int idx(int l, int c) {
     if (W >= 16) return l * W + c;
-    return (l ^ ((l >> 3) & (16 / W - 1))) * W + c;
+    return (l ^ ((l >> 3) & M)) * W + c;
+  }
+  // split addressing: the swizzle only changes bits 0..2 of l and reads bits
+  // 3..5, so a step that is a multiple of 8(M+1) passes through it; the
+  // radix-8 stores of the first two passes swizzle by a per-thread (b & M)
+  // or a compile-time (q & M) value
+  static constexpr bool kFastAddr = true;
+  template <int STEP>
+  static __device__ __forceinline__ int load_addr(int b, int r, int c) {
+    if constexpr (STEP % (8 * (M + 1)) == 0) return idx(b, c) + r * STEP * W;
+    else return idx(b + r * STEP, c);
+  }
+  template <int NS, int R>
+  static __device__ __forceinline__ int store_addr(int base, int q, int c) {
+    if constexpr (M == 0) {
+      return (base + q * NS) * W + c;
+    } else if constexpr (NS % (8 * (M + 1)) == 0) {
+      return idx(base, c) + q * NS * W;
+    } else if constexpr (NS == 1 && R == 8) {  // base = 8b, position 8b + q
+      const int s = (base >> 3) & M;
+      return (base + ((q & M) ^ s)) * W + c + (q & ~M) * W;
+    } else if constexpr (NS == 8 && R == 8) {  // base = 64(b/8) + b%8, position base + 8q
+      return (base ^ (q & M)) * W + c + 8 * q * W;
+    } else {
+      return idx(base + q * NS, c);
+    }
   }
 };
 
@@ -89,6 +115,15 @@ struct RowCfg {  // row pass with W rows per tile
   static constexpr int MINB_RAW = 65536 / (NT * (E <= 8 ? 96 : 128));
   static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
 };
+
+// shared-memory address of element e of thread j (its first-pass position)
+template <int N, class Lay>
+__device__ __forceinline__ int first_pass_addr(int e, int j, int c) {
+  constexpr int R = Plan<N>::R::value[0];
+  constexpr int NB = N / R;
+  const int u = e / R, r = e - u * R;
+  return load_addr<Lay, NB>(j + Plan<N>::TPT * u, r, c);
+}
 
 template <int N>
 __device__ __forceinline__ void load_twiddles(float2* tw, const float2* __restrict__ twg, int nt) {
@@ -158,7 +193,7 @@ __global__ void __launch_bounds__(ColCfg<N, W, LayT>::NT, ColCfg<N, W, LayT>::MI
     const int x = (tile % TPI) * W + c;
     float2 v[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = sT[Lay::idx(elem_pos<N>(e, j), c)];
+    for (int e = 0; e < E; ++e) v[e] = sT[first_pass_addr<N, Lay>(e, j, c)];
     __syncthreads();  // the stage's T region becomes the exchange buffer
     fft_reg<N, Lay, +1>(v, sT, tw, c, j);
 #pragma unroll
@@ -229,7 +264,7 @@ __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
     const int x = (tile % TPI) * W + c;
     float2 v[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = sT[Lay::idx(elem_pos<N>(e, j), c)];
+    for (int e = 0; e < E; ++e) v[e] = sT[first_pass_addr<N, Lay>(e, j, c)];
     __syncthreads();  // the stage's T region becomes the exchange buffer
     fft_reg<N, Lay, +1>(v, sT, tw, c, j);
     float acc = 0.f;
