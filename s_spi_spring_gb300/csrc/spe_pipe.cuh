@@ -142,6 +142,41 @@ __device__ __forceinline__ void pdl_enter() {
 }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
+// Stage one column tile: W columns of T (16-byte chunks of two columns) in
+// the exchange layout, and the matching W amplitude columns.  When the
+// chunks divide evenly over the threads, each thread copies the same column
+// pair at rows y0, y0 + RS, ... so every address is its base plus a
+// compile-time offset.
+template <int N, int W, int NT, class Lay>
+__device__ __forceinline__ void stage_cols(float2* sT, float* sA, const float2* __restrict__ gT,
+                                           const float* __restrict__ gA, int t) {
+  constexpr int CT = N * W / 2, CA = N * W / 4;  // 16-byte chunks of T and of A
+  if constexpr (CT % NT == 0 && NT % (W / 2) == 0) {
+    constexpr int RS = NT / (W / 2);
+    const int y0 = t / (W / 2), h = t - y0 * (W / 2);
+#pragma unroll
+    for (int i = 0; i < CT / NT; ++i)
+      cp_async16(&sT[load_addr<Lay, RS>(y0, i, 2 * h)], gT + (size_t)(y0 + i * RS) * N + 2 * h);
+  } else {
+    for (int q = t; q < CT; q += NT) {
+      const int y = q / (W / 2), h = q - y * (W / 2);
+      cp_async16(&sT[Lay::idx(y, 2 * h)], gT + (size_t)y * N + 2 * h);
+    }
+  }
+  if constexpr (CA % NT == 0 && NT % (W / 4) == 0) {
+    constexpr int RS = NT / (W / 4);
+    const int y0 = t / (W / 4), h = t - y0 * (W / 4);
+#pragma unroll
+    for (int i = 0; i < CA / NT; ++i)
+      cp_async16(&sA[(y0 + i * RS) * W + 4 * h], gA + (size_t)(y0 + i * RS) * N + 4 * h);
+  } else {
+    for (int q = t; q < CA; q += NT) {
+      const int y = q / (W / 4), h = q - y * (W / 4);
+      cp_async16(&sA[y * W + 4 * h], gA + (size_t)y * N + 4 * h);
+    }
+  }
+}
+
 // column pass: T -> FFT+ (y) -> P_M with A -> FFT- (y) -> T
 template <int N, int W, class LayT = LayCol<N, W>>
 __global__ void __launch_bounds__(ColCfg<N, W, LayT>::NT, ColCfg<N, W, LayT>::MINB)
@@ -167,14 +202,7 @@ __global__ void __launch_bounds__(ColCfg<N, W, LayT>::NT, ColCfg<N, W, LayT>::MI
     float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
     const float2* gT = T + (size_t)p * N * N + x0;
     const float* Ap = ipp > 0 ? A + (size_t)(p / ipp) * N * N : A;  // the individual's pattern
-    for (int q = t; q < N * W / 2; q += NT) {
-      const int y = q / (W / 2), h = q - y * (W / 2);
-      cp_async16(&sT[Lay::idx(y, 2 * h)], gT + (size_t)y * N + 2 * h);
-    }
-    for (int q = t; q < N * W / 4; q += NT) {
-      const int y = q / (W / 4), h = q - y * (W / 4);
-      cp_async16(&sA[y * W + 4 * h], Ap + (size_t)y * N + x0 + 4 * h);
-    }
+    stage_cols<N, W, NT, Lay>(sT, sA, gT, Ap + x0, t);
   };
 
   int tile = blockIdx.x;
@@ -238,14 +266,7 @@ __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
     float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
     const float2* gT = T + (size_t)p * N * N + x0;
     const float* Ap = ipp > 0 ? A + (size_t)(p / ipp) * N * N : A;
-    for (int q = t; q < N * W / 2; q += NT) {
-      const int y = q / (W / 2), h = q - y * (W / 2);
-      cp_async16(&sT[Lay::idx(y, 2 * h)], gT + (size_t)y * N + 2 * h);
-    }
-    for (int q = t; q < N * W / 4; q += NT) {
-      const int y = q / (W / 4), h = q - y * (W / 4);
-      cp_async16(&sA[y * W + 4 * h], Ap + (size_t)y * N + x0 + 4 * h);
-    }
+    stage_cols<N, W, NT, Lay>(sT, sA, gT, Ap + x0, t);
   };
 
   int tile = blockIdx.x;
