@@ -761,7 +761,7 @@ int spe_sequence(spe_engine* e, int first, int count, const spe_op* ops, int nop
 
 int spe_set_tiles(spe_engine* e, int cols, int rows) {
   if (!e) return fail(SPE_ERR_INVALID, "null engine");
-  int w[16];
+  int w[32];
   auto ok = [&](int v, int (*f)(int*)) {
     if (v == 0) return true;
     const int k = f(w);
@@ -950,7 +950,7 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
     return SPE_OK;
   };
   auto trial = [&](int wc, int wr, float* ms) { return trial_s(wc, wr, 0, 1, ms); };
-  int wcs[16], wrs[16];
+  int wcs[32], wrs[32];
   const int nc = e->ops->col_widths(wcs), nr = e->ops->row_widths(wrs);
   int best_c = e->tile_cols != 0 ? e->tile_cols : e->ops->default_cols;
   int best_r = e->tile_rows > 0 ? e->tile_rows : e->ops->default_rows;
