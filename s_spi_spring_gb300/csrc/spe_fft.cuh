@@ -218,7 +218,11 @@ struct LayPad {  // row passes
 
 // ---------------------------------------------------------------------------
 // radix plans.  TPT threads per sequence, E = L/TPT elements per thread;
-// every radix divides E; the first and the last radix are equal.
+// every radix divides E; the first and the last radix are equal.  E is kept
+// at 8 (12 where the side has a factor 3) even at the price of a fourth
+// pass: a stage of a pass holds about 20 bytes per element (T, the previous
+// iterate and the support) twice, so the threads an SM can keep resident
+// fall as 1/E, and at E = 16 or 24 the row pass ran with 4 to 6 warps per SM.
 // ---------------------------------------------------------------------------
 template <int... Rs>
 struct Radices {
@@ -234,11 +238,11 @@ template <> struct Plan<32>   { static constexpr int TPT = 4;   using R = Radice
 template <> struct Plan<64>   { static constexpr int TPT = 8;   using R = Radices<8, 8>; };
 template <> struct Plan<128>  { static constexpr int TPT = 16;  using R = Radices<4, 8, 4>; };
 template <> struct Plan<256>  { static constexpr int TPT = 32;  using R = Radices<8, 4, 8>; };
-template <> struct Plan<384>  { static constexpr int TPT = 16;  using R = Radices<8, 6, 8>; };
+template <> struct Plan<384>  { static constexpr int TPT = 32;  using R = Radices<4, 6, 4, 4>; };
 template <> struct Plan<512>  { static constexpr int TPT = 64;  using R = Radices<8, 8, 8>; };
-template <> struct Plan<768>  { static constexpr int TPT = 32;  using R = Radices<8, 12, 8>; };
-template <> struct Plan<1024> { static constexpr int TPT = 64;  using R = Radices<8, 16, 8>; };
-template <> struct Plan<2048> { static constexpr int TPT = 128; using R = Radices<16, 8, 16>; };
+template <> struct Plan<768>  { static constexpr int TPT = 64;  using R = Radices<4, 12, 4, 4>; };
+template <> struct Plan<1024> { static constexpr int TPT = 128; using R = Radices<8, 4, 4, 8>; };
+template <> struct Plan<2048> { static constexpr int TPT = 256; using R = Radices<8, 8, 4, 8>; };
 // clang-format on
 
 // Per-pass twiddle table of a plan: for every pass after the first (NS > 1)
@@ -411,11 +415,14 @@ __device__ __forceinline__ int elem_pos(int e, int j) {
   return (j + Plan<L>::TPT * u) + r * NB;
 }
 
-// Tile widths (sequences per CTA) of the two passes.
+// Tile widths (sequences per CTA) of the two passes, at most 1024 threads.
 template <int L>
 struct TileW {
-  static constexpr int rows = (L >= 1024) ? 4 : (L >= 256 ? 8 : 16);
-  static constexpr int cols = (L >= 512) ? 8 : 16;
+  static constexpr int cap = 1024 / Plan<L>::TPT;
+  static constexpr int rows0 = (L >= 1024) ? 4 : (L >= 256 ? 8 : 16);
+  static constexpr int cols0 = (L >= 512) ? 8 : 16;
+  static constexpr int rows = rows0 < cap ? rows0 : cap;
+  static constexpr int cols = cols0 < cap ? cols0 : cap;
 };
 
 }  // namespace spe
