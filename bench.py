@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--large", type=int, default=1, help="time the 2048^2 x 128 population (0: skip)")
     ap.add_argument("--refine", type=int, default=1, help="time the gradient-refinement epoch (0: skip)")
     ap.add_argument("--profile-loss", action="store_true", help="profiling case: one loss + gradient at 512^2 x 64")
+    ap.add_argument("--profile-sizes", action="store_true",
+                    help="profiling case: two RAAR iterations per pattern side 256..2048")
     ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
     ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
@@ -719,10 +721,36 @@ def run_profile_case(args):
     print(json.dumps({"profile_case": "RAAR", "iterations": args.profile_iters, "tiles": tiles, "schedule": sched}))
 
 
+PROFILE_SIDES = (256, 384, 512, 768, 1024, 2048)
+
+
+def run_profile_sizes():
+    """Two RAAR iterations per pattern side, default tiles, one stream, on a
+    population of about 8.4 M pixels per side with device-synthesised objects
+    (for per-side ncu launch lists)."""
+    from s_spi_spring_gb300 import _lib, synthetic
+    for n in PROFILE_SIDES:
+        P = max(2, int(round(8.4e6 / (n * n))))
+        I, _, _ = synthetic.polygon_pattern(seed=3, n=n, diameter=n * 0.23, photons=1e8, stop_radius=max(2, n // 64))
+        eng = _lib.Engine(n, 0)
+        eng.set_amplitudes(_lib.prepare_pattern(I, (-1, -1), True))
+        eng.reserve(P)
+        eng.seed(7)
+        ss = int(n * 0.3)
+        eng.initialize_pop(0, P, ss, (ss * 0.2, ss * 0.9), (2, 8), (0.5, 0.5), (0.5, 1.5), 0.0)
+        eng.raar(0, P, 2, BETA, 0.0)
+        eng.synchronize()
+        eng.close()
+        print(json.dumps({"profile_case": "RAAR per side", "n": n, "population": P, "iterations": 2}))
+
+
 def main():
     args = parse()
     if args.profile_iters > 0:
         run_profile_case(args)
+        return
+    if args.profile_sizes:
+        run_profile_sizes()
         return
     if args.profile_loss:
         run_profile_loss()

@@ -111,9 +111,9 @@ constexpr int kRowWidths[5] = {1, 2, 4, 8, 16};
 
 // default widths (before any tuning)
 template <int N>
-struct DefaultTiles {
-  static constexpr int cols = (N >= 2048) ? 4 : (N >= 512 ? 8 : 16);
-  static constexpr int rows = (N <= 256) ? 8 : (N == 384 ? 8 : (N <= 512 ? 4 : (N <= 1024 ? 2 : 1)));
+struct DefaultTiles {  // what the autotuner picks for a population of ~32 M pixels
+  static constexpr int cols = (N >= 2048) ? 4 : (N >= 512 || N == 256 ? 8 : 16);
+  static constexpr int rows = (N <= 256) ? 8 : (N == 384 ? 2 : (N <= 512 ? 4 : 1));
 };
 
 // persistent grid size: the CTAs that fit on all SMs at once (occupancy
