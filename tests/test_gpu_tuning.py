@@ -25,7 +25,7 @@ def engine(n, P, seed=0):
     return e, dens, S
 
 
-@pytest.mark.parametrize("n", [64, 128, 256, 384, 512, 1024])
+@pytest.mark.parametrize("n", [64, 128, 256, 384, 512, 768, 1024, 2048])
 def test_all_tile_widths_bit_identical(n):
     P = 3
     e, dens, S = engine(n, P)
