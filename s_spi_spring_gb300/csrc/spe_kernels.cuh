@@ -322,13 +322,13 @@ __device__ __forceinline__ float2 update(float2 rp, float2 prev, int s, float be
   } else if (UPD == UPD_HIO) {
     const float t = phase_out(rp, g) ? 0.f : (float)s;
     const float u = 1.f - t;
-    return make_float2(fmaf(fmaf(-beta, rp.x, prev.x), u, rp.x * t),
-                       fmaf(fmaf(-beta, rp.y, prev.y), u, rp.y * t));
+    const float2 q = __ffma2_rn(make_float2(-beta, -beta), rp, prev);  // prev - beta rp
+    return make_float2(fmaf(q.x, u, rp.x * t), fmaf(q.y, u, rp.y * t));
   } else {
     const float2 refl = make_float2(2.f * rp.x - prev.x, 2.f * rp.y - prev.y);
     if (s == 0 || phase_out(refl, g)) {
       const float k = 1.f - 2.f * beta;
-      return make_float2(fmaf(beta, prev.x, k * rp.x), fmaf(beta, prev.y, k * rp.y));
+      return __ffma2_rn(make_float2(beta, beta), prev, __fmul2_rn(make_float2(k, k), rp));
     }
     return rp;
   }

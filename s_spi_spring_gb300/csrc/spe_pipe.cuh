@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(RowCfg<N, W>::NT, RowCfg<N, W>::MINB)
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int l = elem_pos<N>(e, j);
-      const float2 rp = make_float2(v[e].x * scale, v[e].y * scale);
+      const float2 rp = __fmul2_rn(v[e], make_float2(scale, scale));
       const float2 prev = NEED_PREV ? sR[c * N + l] : make_float2(0.f, 0.f);
       const float2 r = update<UPD>(rp, prev, sS[c * N + l], beta, g);
       rho[rowbase + l] = r;
