@@ -220,6 +220,84 @@ struct LayPad {  // row passes
   }
 };
 
+// Row exchange layout with a padding chosen per exchange: slot of position l
+// in the exchange after the pass of output stride NS is
+//   l + A(NS) (l >> 4) + B(NS) (l >> 6)
+// in a row of STRIDE slots.  The table picks, per side and exchange, the
+// padding under which the exchange's Stockham stores and the next pass's
+// loads are conflict-free for every half-warp (8-byte accesses are served 16
+// lanes at a time); where no padding of this family is, it keeps l + l/16.
+// Every address stays a per-thread base plus a compile-time offset.  A
+// row-pass variant (tile codes 100 + W): fewer bank conflicts, but a wider
+// row, and which one is faster depends on the tile and the schedule.
+template <int L>
+struct RowPads {
+  // {NS, A, B} per exchange; unlisted exchanges use A = 1, B = 0
+  // (at 2048 the wider row of the conflict-free second exchange would push
+  // the one-row CTA of the row pass past two per SM, so 2048 keeps l + l/16)
+  static constexpr int n = (L == 512 || L == 1024 || L == 768 || L == 384) ? 1 : 0;
+  __host__ __device__ static constexpr int ns_at(int) {
+    return L == 512 ? 8 : L == 1024 ? 32 : L == 768 ? 48 : L == 384 ? 24 : 0;
+  }
+  __host__ __device__ static constexpr int a(int ns) {
+    for (int i = 0; i < n; ++i)
+      if (ns_at(i) == ns) return 0;
+    return 1;
+  }
+  __host__ __device__ static constexpr int b(int ns) {
+    if (L == 512 && ns == 8) return 8;
+    if (L == 384 && ns == 24) return 8;
+    return 0;
+  }
+  __host__ __device__ static constexpr int extent(int ns) {
+    return (L - 1) + a(ns) * ((L - 1) >> 4) + b(ns) * ((L - 1) >> 6) + 1;
+  }
+  __host__ __device__ static constexpr int stride() {  // at least the l + l/16 row of LayPad
+    int s = L + L / 16 > extent(1) ? L + L / 16 : extent(1);
+    for (int i = 0; i < n; ++i) s = extent(ns_at(i)) > s ? extent(ns_at(i)) : s;
+    return s;
+  }
+};
+
+template <int L, int W>
+struct LayRowX {
+  using Pads = RowPads<L>;
+  static constexpr int STRIDE = Pads::stride();
+  static constexpr int SIZE = W * STRIDE;
+  template <int NS>
+  static __device__ __forceinline__ int idx_x(int l, int c) {
+    constexpr int A = Pads::a(NS), B = Pads::b(NS);
+    return c * STRIDE + l + A * (l >> 4) + B * (l >> 6);
+  }
+  static constexpr bool kFastAddr = true;
+  static constexpr bool kPerExchange = true;
+  template <int NS, int R>
+  static __device__ __forceinline__ int store_addr(int base, int q, int c) {
+    constexpr int A = Pads::a(NS), B = Pads::b(NS);
+    if constexpr (NS == 1 && 16 % R == 0) {  // base = R b: q never carries into bit 4
+      return idx_x<NS>(base, c) + q;
+    } else if constexpr (NS % 64 == 0 || (B == 0 && NS % 16 == 0)) {
+      return idx_x<NS>(base, c) + q * (NS + A * (NS / 16) + B * (NS / 64));
+    } else if constexpr (NS == 8 && R == 8) {  // base = 64 (b / 8) + b % 8, position base + 8 q
+      return idx_x<NS>(base, c) + 8 * q + A * (q >> 1);
+    } else {
+      return idx_x<NS>(base + q * NS, c);
+    }
+  }
+  template <int STEP, int NS>
+  static __device__ __forceinline__ int load_addr_x(int b, int r, int c) {
+    constexpr int A = Pads::a(NS), B = Pads::b(NS);
+    if constexpr (STEP % 64 == 0 || (B == 0 && STEP % 16 == 0))
+      return idx_x<NS>(b, c) + r * (STEP + A * (STEP / 16) + B * (STEP / 64));
+    else
+      return idx_x<NS>(b + r * STEP, c);
+  }
+  template <int STEP>
+  static __device__ __forceinline__ int load_addr(int b, int r, int c) {
+    return load_addr_x<STEP, 1>(b, r, c);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // radix plans.  TPT threads per sequence, E = L/TPT elements per thread;
 // every radix divides E; the first and the last radix are equal.  E is kept
@@ -339,6 +417,20 @@ __device__ __forceinline__ int load_addr(int b, int r, int c) {
   else return Lay::idx(b + r * STEP, c);
 }
 
+// A layout may also arrange each exchange differently (announced by
+// kPerExchange): the exchange after the pass whose outputs have stride NS
+// uses the arrangement for NS, so the loads of the next pass take NS too.
+template <class Lay, class = void>
+struct HasPerExchange : std::false_type {};
+template <class Lay>
+struct HasPerExchange<Lay, std::void_t<decltype(Lay::kPerExchange)>> : std::true_type {};
+
+template <class Lay, int STEP, int NS>
+__device__ __forceinline__ int load_addr_x(int b, int r, int c) {
+  if constexpr (HasPerExchange<Lay>::value) return Lay::template load_addr_x<STEP, NS>(b, r, c);
+  else return load_addr<Lay, STEP>(b, r, c);
+}
+
 template <int L, int TPT, int S, class Lay, int P, int NS, class Sync = SyncCTA>
 __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf, const float2* __restrict__ tw,
                                              int c, int j) {
@@ -381,7 +473,7 @@ __device__ __forceinline__ void fft_pass_reg(float2* v, float2* __restrict__ buf
     for (int u = 0; u < U2; ++u) {
       const int b = j + TPT * u;
 #pragma unroll
-      for (int r = 0; r < R2; ++r) v[u * R2 + r] = buf[load_addr<Lay, NB2>(b, r, c)];
+      for (int r = 0; r < R2; ++r) v[u * R2 + r] = buf[load_addr_x<Lay, NB2, NS>(b, r, c)];
     }
     Sync::sync(c);
     fft_pass_reg<L, TPT, S, Lay, P + 1, NS * R, Sync>(v, buf, tw, c, j);

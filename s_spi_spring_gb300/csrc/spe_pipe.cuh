@@ -98,8 +98,8 @@ struct ColCfg {  // column pass with W columns per tile
   static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
 };
 
-template <int N, int W>
-struct RowCfg {  // row pass with W rows per tile
+template <int N, int W, class XLay = LayPad<N, W>>
+struct RowCfg {  // row pass with W rows per tile, exchanges in layout XLay
   static constexpr int TPT = Plan<N>::TPT;
   static constexpr int E = Elems<N>::value;
   static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
@@ -110,7 +110,7 @@ struct RowCfg {  // row pass with W rows per tile
   static constexpr int R_R = align128(N * W * 8);
   static constexpr int R_S = align128(N * W * 4);
   static constexpr int STAGE = R_T + R_R + R_S;
-  static constexpr int R_X = align128(LayPad<N, W>::SIZE * 8);
+  static constexpr int R_X = align128(XLay::SIZE * 8);
   static constexpr size_t SMEM = (size_t)TWB + R_X + 2 * STAGE;
   static constexpr int MINB_RAW = 65536 / (NT * (E <= 8 ? 96 : 128));
   static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
@@ -317,13 +317,13 @@ __global__ void __launch_bounds__(ColCfg<N, W>::NT, ColCfg<N, W>::MINB)
 }
 
 // row pass: T -> FFT- (x) -> /N^2 -> update with (rho, S) -> rho -> FFT+ (x) -> T
-template <int N, int W, int UPD>
-__global__ void __launch_bounds__(RowCfg<N, W>::NT, RowCfg<N, W>::MINB)
+template <int N, int W, int UPD, class XLay = LayPad<N, W>>
+__global__ void __launch_bounds__(RowCfg<N, W, XLay>::NT, RowCfg<N, W, XLay>::MINB)
     k_rows_iterate(float2* __restrict__ T, float2* __restrict__ rho, const int* __restrict__ S, int first,
                    int count, float scale, float beta, Gate g, const float2* __restrict__ twg) {
-  using C = RowCfg<N, W>;
+  using C = RowCfg<N, W, XLay>;
   constexpr int NT = C::NT, E = C::E, TPT = C::TPT, TPI = N / W;
-  using Lay = LayPad<N, W>;
+  using Lay = XLay;
   extern __shared__ __align__(128) unsigned char sm[];
   float2* tw = reinterpret_cast<float2*>(sm);
   float2* xb = reinterpret_cast<float2*>(sm + C::TWB);

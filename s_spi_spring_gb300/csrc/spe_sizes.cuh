@@ -66,10 +66,16 @@ constexpr bool col_ok() {
   return W <= N && N % W == 0 && ColCfg<N, W>::NT % 32 == 0 && ColCfg<N, W>::NT <= 1024 &&
          ColCfg<N, W>::SMEM <= kMaxSmem;
 }
-template <int N, int W>
+template <int N, int W, class XLay = LayPad<N, W>>
 constexpr bool row_ok() {
-  return W <= N && N % W == 0 && RowCfg<N, W>::NT % 32 == 0 && RowCfg<N, W>::NT <= 1024 &&
-         RowCfg<N, W>::SMEM <= kMaxSmem;
+  return W <= N && N % W == 0 && RowCfg<N, W, XLay>::NT % 32 == 0 && RowCfg<N, W, XLay>::NT <= 1024 &&
+         RowCfg<N, W, XLay>::SMEM <= kMaxSmem;
+}
+// the row pass with per-exchange paddings (LayRowX), where they differ from
+// the plain l + l/16 layout
+template <int N, int W>
+constexpr bool xrow_ok() {
+  return RowPads<N>::n > 0 && row_ok<N, W, LayRowX<N, W>>();
 }
 // two-columns-per-thread variants (registers for 2E elements): E <= 8 only
 template <int N, int W>
@@ -169,10 +175,10 @@ cudaError_t launch_cols_project(const Ctx& c) {
   return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, c.tw);
 }
 
-template <int N, int W, int UPD>
+template <int N, int W, int UPD, class XLay = LayPad<N, W>>
 cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
-  using P = RowCfg<N, W>;
-  auto kern = k_rows_iterate<N, W, UPD>;
+  using P = RowCfg<N, W, XLay>;
+  auto kern = k_rows_iterate<N, W, UPD, XLay>;
   static unsigned long long configured = 0ull;
   static int resident[64] = {0};
   cudaError_t e = configure(kern, P::SMEM, configured);
@@ -260,6 +266,10 @@ cudaError_t launch_rows_w(const Ctx& c, int w, float scale, float beta, Gate g) 
     case 4: if constexpr (row_ok<N, 4>()) return launch_rows_iterate<N, 4, UPD>(c, scale, beta, g); break;
     case 8: if constexpr (row_ok<N, 8>()) return launch_rows_iterate<N, 8, UPD>(c, scale, beta, g); break;
     case 16: if constexpr (row_ok<N, 16>()) return launch_rows_iterate<N, 16, UPD>(c, scale, beta, g); break;
+    case 101: if constexpr (xrow_ok<N, 1>()) return launch_rows_iterate<N, 1, UPD, LayRowX<N, 1>>(c, scale, beta, g); break;
+    case 102: if constexpr (xrow_ok<N, 2>()) return launch_rows_iterate<N, 2, UPD, LayRowX<N, 2>>(c, scale, beta, g); break;
+    case 104: if constexpr (xrow_ok<N, 4>()) return launch_rows_iterate<N, 4, UPD, LayRowX<N, 4>>(c, scale, beta, g); break;
+    case 108: if constexpr (xrow_ok<N, 8>()) return launch_rows_iterate<N, 8, UPD, LayRowX<N, 8>>(c, scale, beta, g); break;
     default: break;
   }
   return cudaErrorInvalidValue;
@@ -362,6 +372,10 @@ struct SizeImpl {
     if constexpr (row_ok<N, 4>()) out[k++] = 4;
     if constexpr (row_ok<N, 8>()) out[k++] = 8;
     if constexpr (row_ok<N, 16>()) out[k++] = 16;
+    if constexpr (xrow_ok<N, 1>()) out[k++] = 101;
+    if constexpr (xrow_ok<N, 2>()) out[k++] = 102;
+    if constexpr (xrow_ok<N, 4>()) out[k++] = 104;
+    if constexpr (xrow_ok<N, 8>()) out[k++] = 108;
     return k;
   }
 

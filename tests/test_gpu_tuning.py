@@ -31,7 +31,8 @@ def test_all_tile_widths_bit_identical(n):
     e, dens, S = engine(n, P)
     ref = None
     tried = 0
-    for wc, wr in itertools.product([4, 8, 16, -4, -8, -16, 104, 108, 116, 204, 208, 304, 308], [1, 2, 4, 8, 16]):
+    for wc, wr in itertools.product([4, 8, 16, -4, -8, -16, 104, 108, 116, 204, 208, 304, 308],
+                                    [1, 2, 4, 8, 16, 101, 102, 104, 108]):
         try:
             e.set_tiles(wc, wr)
         except _lib.EngineError:
