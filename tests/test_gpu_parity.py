@@ -2,9 +2,13 @@
 
 Tolerances (float32 engine vs float64 oracle, relative L2 over each
 individual): one projection / one iteration 2e-6; 5 iterations: median over
-the individuals 1e-4, every individual 1e-2 (ER 2e-5; most individuals stay
-near 1e-5, single ones reach a few 1e-3 when a pixel's phase sits on the
-+-pi gate boundary and the difference is then amplified).  From a random start HIO and RAAR amplify rounding differences by
+the individuals 1e-4 (ER 2e-5), every individual 1e-2 (most individuals stay
+near 1e-5; single ones reach a few 1e-3 when a pixel's phase sits on the
+gate boundary, so that the float32 and float64 decisions differ for that
+pixel, and the difference is then carried by the transforms: with ER, a
+reality gate of 0.5 and n = 1024 one small pixel (|rho| ~ 4e-5) differs
+after iteration 2 and its neighbours' gate decisions follow, 10 pixels and
+2e-3 by iteration 5).  From a random start HIO and RAAR amplify rounding differences by
 roughly 2x per iteration (their out-of-support update is expansive; the
 float32 C restatement diverges from the float64 oracle at the same rate), so
 longer runs are compared through the R-factor: the trajectory over 20
@@ -75,13 +79,13 @@ def test_projection_matches_oracle(n):
 ALGS = [("HIO", 0.9), ("RAAR", 0.87), ("ER", 0.0)]
 
 
-@pytest.mark.parametrize("n", [64, 128, 384, 512])
+@pytest.mark.parametrize("n", [64, 128, 384, 512, 768, 1024])
 @pytest.mark.parametrize("alg,beta", ALGS)
 @pytest.mark.parametrize("reality", [0.0, 0.5])
 def test_iterations_match_oracle(n, alg, beta, reality):
     A, dens, S = setup_case(n, 3, seed=n + 7)
     e = make_engine(n, A, dens, S)
-    for iters, tol in ((1, 2e-6), (5, 2e-5 if alg == "ER" else 1e-2)):
+    for iters, tol in ((1, 2e-6), (5, 1e-2)):
         e.upload(0, dens, S)
         if alg == "HIO":
             e.hio(0, 3, iters, beta, reality)
