@@ -6,7 +6,7 @@ import gc
 import numpy as np
 import pytest
 
-from s_spi_spring_gb300 import _lib, synthetic
+from s_spi_spring_gb300 import synthetic
 from s_spi_spring_gb300.spring_core.phase_retrieval import Reconstruction, Solver
 
 pytestmark = pytest.mark.gpu

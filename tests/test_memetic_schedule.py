@@ -4,7 +4,6 @@ tests/golden/make_schedule_golden.py from spring/alg_manager.py)."""
 import json
 import os
 
-import numpy as np
 import pytest
 
 from s_spi_spring_gb300.memetic import MemeticSettings
