@@ -420,12 +420,14 @@ def refinement(args, local):
 
 def large_population(args, local):
     """Large population: 2048 x 2048 complex64, 128 individuals (about 17 GB
-    of device state), starting population synthesised on the device
+    of device state); the object a seeded cluster of 3-8 overlapping
+    ellipsoid projections, 1e9 photons, a beamstop and a gap grid masking 25%
+    of the pixels; starting population synthesised on the device
     (spe_initialize_pop), RAAR beta 0.87; timed over 20 iterations."""
     import torch
     from s_spi_spring_gb300 import _lib, synthetic
     n, P, iters = 2048, 128, 20
-    I, _, _ = synthetic.polygon_pattern(seed=9, n=n, diameter=480.0, photons=1e9, stop_radius=12, gap=6, stripes=3)
+    I, _, _ = synthetic.ellipsoid_cluster_pattern(seed=9, n=n, extent=480.0, photons=1e9, masked=0.25)
     eng = _lib.Engine(n, local)
     eng.set_amplitudes(_lib.prepare_pattern(I, (-1, -1), True))
     eng.reserve(P)
@@ -447,7 +449,8 @@ def large_population(args, local):
     peak, kind = peaks()
     alg = B_PER_PIXEL_ITER * n * n * P * iters
     eng.close()
-    return {"workload": "2048x2048 complex64, 128 individuals, RAAR beta 0.87", "iterations": iters,
+    return {"workload": "2048x2048 complex64, 128 individuals, RAAR beta 0.87; ellipsoid-cluster object, "
+                        "1e9 photons, 25% of pixels masked", "iterations": iters,
             "ms_per_iteration": round(ms / iters, 3), "iter_ind_per_s": round(P * iters / (ms / 1e3), 1),
             "alg_gbps": round(alg / (ms / 1e3) / 1e9, 1), "frac": round(alg / (ms / 1e3) / 1e9 / peak, 4),
             "device_state_gb": round(P * n * n * 32 / 1e9, 1), "tiles": list(tiles), "schedule": list(sched),

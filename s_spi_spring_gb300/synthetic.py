@@ -95,6 +95,44 @@ def polygon_pattern(seed: int = 1, n: int = 512, diameter: float = 120.0, photon
     return I, obj.astype(np.complex64), supp.astype(np.int32)
 
 
+def ellipsoid_cluster_pattern(seed: int = 1, n: int = 2048, extent: float = 480.0, photons: float = 1e9,
+                              masked: float = 0.25, stop_radius: float = 12.0):
+    """Seeded cluster of 3-8 overlapping uniform ellipsoids, projected along
+    the beam: each adds density d * sqrt(1 - (u/a)^2 - (v/b)^2) over its
+    in-plane ellipse (semi-axes a, b, random orientation, centres within
+    `extent` pixels), d uniform in [0.2, 1]; the sum is scaled to a maximum
+    of 1.  Poisson intensities with `photons` in total; a masked central disc
+    plus a grid of detector gaps (period n/8, width chosen so that about
+    `masked` of the pixels are missing).  Returns (intensities, true_object,
+    true_support)."""
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(3, 9))
+    yy, xx = np.mgrid[0:n, 0:n] + 0.5
+    rho = np.zeros((n, n))
+    c = n / 2
+    for _ in range(k):
+        cx, cy = c + rng.uniform(-0.25, 0.25, 2) * extent
+        a, b = rng.uniform(0.12, 0.3, 2) * extent
+        t = rng.uniform(0, math.pi)
+        u = (xx - cx) * math.cos(t) + (yy - cy) * math.sin(t)
+        v = -(xx - cx) * math.sin(t) + (yy - cy) * math.cos(t)
+        q = 1.0 - (u / a) ** 2 - (v / b) ** 2
+        rho += rng.uniform(0.2, 1.0) * np.sqrt(np.clip(q, 0.0, None))
+    rho /= rho.max()
+    supp = rho > 0
+    obj = rho.astype(np.complex128)
+    I = _intensity(obj, photons, rng)
+    period = n // 8
+    width = max(1, int(round(period * (1.0 - math.sqrt(1.0 - masked)))))
+    r = np.arange(n)
+    gap = (r % period) >= period - width
+    I[gap, :] = -1.0
+    I[:, gap] = -1.0
+    iy, ix = np.mgrid[0:n, 0:n]
+    I[((ix - n // 2) ** 2 + (iy - n // 2) ** 2) <= stop_radius ** 2] = -1.0
+    return I, obj.astype(np.complex64), supp.astype(np.int32)
+
+
 def start_population(n: int, count: int, radius: float, seed: int = 0):
     """Random starting guesses: uniform random complex values on a centred
     disc support of the given radius.  Returns (densities, supports)."""
