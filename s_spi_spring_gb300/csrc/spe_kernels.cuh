@@ -634,11 +634,15 @@ __device__ __forceinline__ float loss_term(float2 F, float a, float eps, float2*
     if (g) *g = make_float2(f * F.x, f * F.y);
     return d * d;
   } else {
+    // the hardware logarithm and reciprocal (a few ulp) instead of the
+    // IEEE-rounded logf and division: the loss and the gradient stay within
+    // the errors stated against the FP64 oracle, at a third of the
+    // instructions of this term
     const float i = a * a;
     const float den = m2 + eps;
-    const float f = 2.f * (1.f - i / den);
+    const float f = 2.f * (1.f - __fdividef(i, den));
     if (g) *g = make_float2(f * F.x, f * F.y);
-    return m2 - i * logf(den);
+    return m2 - i * __logf(den);
   }
 }
 
