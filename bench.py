@@ -541,7 +541,7 @@ def run_engine(args):
                   0.0, fp(h_out), E2E_BLOCKS)
 
     def e2e_time(step):
-        for _ in range(max(1, args.warmup // 2)):
+        for _ in range(max(1, args.warmup)):
             step()
         barrier()
         torch.cuda.synchronize()
