@@ -44,6 +44,9 @@ int main(int argc, char** argv) {
   spe_engine* e = NULL;
   CHECK(spe_create(n, 0, &e));
   CHECK(spe_set_amplitudes(e, A));
+  /* slots must be reserved before use; an upload past the capacity fails */
+  if (spe_upload(e, 0, P, NULL, NULL) == SPE_OK) return 7;
+  CHECK(spe_reserve(e, P));
   float* rho = malloc(2 * np * P * sizeof(float));
   int32_t* S = malloc(np * P * sizeof(int32_t));
   for (size_t i = 0; i < np * P; ++i) {
