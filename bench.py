@@ -585,6 +585,9 @@ def run_engine(args):
                                        "profiles/k_rows_iterate_raar512_pop64.md)",
                      "kernel": "fused iteration (column pass + row pass), per iteration",
                      "alg_bytes_per_launch": alg_bytes, "ms_per_iteration": round(t_iter_ms, 5),
+                     # the DRAM rate the measured traffic implies at this iteration time
+                     "traffic_gbps": round(ITER_DRAM_BYTES / (t_iter_ms / 1e3) / 1e9, 1),
+                     "traffic_frac": round(ITER_DRAM_BYTES / (t_iter_ms / 1e3) / 1e9 / peak, 4),
                      "peak_source": peak_kind},
         "gpu_launches": args.steps * (2 * args.iters + 3) * (-(-POP // sched[0]) if sched[0] > 0 else 1),
         "clocks": clocks.summary(),
