@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--profile-loss", action="store_true", help="profiling case: one loss + gradient at 512^2 x 64")
     ap.add_argument("--profile-sizes", action="store_true",
                     help="profiling case: two RAAR iterations per pattern side 256..2048")
+    ap.add_argument("--profile-memetic", action="store_true",
+                    help="profiling case: one memetic generation at 512^2 x 64 through the Solver")
     ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
     ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
@@ -749,6 +751,29 @@ def run_profile_sizes():
         print(json.dumps({"profile_case": "RAAR per side", "n": n, "population": P, "iterations": 2}))
 
 
+def run_profile_memetic():
+    """One generation of the memetic loop on the population workload through
+    the Solver front end (after the loop's start), for ncu launch lists."""
+    import torch
+    from s_spi_spring_gb300 import synthetic
+    from s_spi_spring_gb300.memetic import MemeticRun, MemeticSettings
+    from s_spi_spring_gb300.spring_core.phase_retrieval import Solver
+    I, _, _ = synthetic.polygon_pattern(seed=1, n=N, diameter=120.0, photons=1e7, stop_radius=8, gap=4, stripes=2)
+    st = MemeticSettings(generations=10, popsize=POP, alg="RAAR", it=100, beta=BETA, it_ER=20, it_eval=20,
+                         sigma=3.0, threshold=0.1)
+    sol = Solver(I, gpus=[0], seed=42)
+    sol.engine.set_tiles(8, 104)
+    sol.engine.set_schedule(32, 2)
+    recs = sol.InitializePop(POP, 128, itemsize=[128 * 0.2, 128 * 0.9], nitems=[2, 8], exponent=[0.5, 0.5],
+                             scaling=[0.5, 1.5], phaserange=0)
+    run = MemeticRun(sol, recs, st)
+    run.start()
+    run.step()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "one memetic generation", "n": N, "population": POP,
+                      "sequence": run.algman.sequence(run.generation, area=[1, 1])}))
+
+
 def main():
     args = parse()
     if args.profile_iters > 0:
@@ -756,6 +781,9 @@ def main():
         return
     if args.profile_sizes:
         run_profile_sizes()
+        return
+    if args.profile_memetic:
+        run_profile_memetic()
         return
     if args.profile_loss:
         run_profile_loss()
