@@ -63,6 +63,7 @@ def parse():
                     help="profiling case: two RAAR iterations per pattern side 256..2048")
     ap.add_argument("--profile-memetic", action="store_true",
                     help="profiling case: one memetic generation at 512^2 x 64 through the Solver")
+    ap.add_argument("--pop-sweep", action="store_true", help="iteration rate against population size at 512^2")
     ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
     ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
@@ -774,6 +775,40 @@ def run_profile_memetic():
                       "sequence": run.algman.sequence(run.generation, area=[1, 1])}))
 
 
+def run_pop_sweep(args):
+    """Iteration rate against population size at 512^2 (RAAR 100 per call,
+    autotuned per population, CUDA events, median of 5 calls)."""
+    import torch
+    from s_spi_spring_gb300 import _lib, synthetic
+    I, _, _ = synthetic.polygon_pattern(seed=1, n=N, diameter=120.0, photons=1e7, stop_radius=8, gap=4, stripes=2)
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    out = []
+    for P in (1, 4, 16, 32, 64, 128, 256):
+        dens, S = synthetic.start_population(N, P, 70.0, seed=2)
+        eng = _lib.Engine(N, 0)
+        eng.set_amplitudes(A)
+        stream = torch.cuda.Stream()
+        eng.set_stream(stream.cuda_stream)
+        eng.upload(0, dens, S)
+        eng.autotune(0, P, 10)
+        for _ in range(2):
+            eng.raar(0, P, args.iters, BETA, 0.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ts = []
+        for _ in range(5):
+            e0.record(stream)
+            eng.raar(0, P, args.iters, BETA, 0.0)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = sorted(ts)[2]
+        out.append({"population": P, "iter_ind_per_s": round(P * args.iters / (ms / 1e3), 1),
+                    "ms_per_iteration": round(ms / args.iters, 4), "tiles": list(eng.tiles()),
+                    "schedule": list(eng.schedule())})
+        eng.close()
+    print(json.dumps({"sweep": "population at 512^2, RAAR", "points": out}))
+
+
 def main():
     args = parse()
     if args.profile_iters > 0:
@@ -784,6 +819,9 @@ def main():
         return
     if args.profile_memetic:
         run_profile_memetic()
+        return
+    if args.pop_sweep:
+        run_pop_sweep(args)
         return
     if args.profile_loss:
         run_profile_loss()

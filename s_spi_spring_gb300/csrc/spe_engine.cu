@@ -940,8 +940,9 @@ int spe_get_tiles(spe_engine* e, int* cols, int* rows) {
 // population [first, first+count) (RAAR, `iterations` per trial, median of
 // three) -- first the column pass with the current row width, then every row
 // width with every schedule (whole range, or blocks on one or two lanes; a
-// blocked schedule is kept only when 2% faster) -- keeps the fastest and
-// restores the densities.
+// blocked schedule is kept only when 2% faster than the best whole-range
+// one, the two re-timed over three times the iterations when they are within
+// 5%) -- keeps the fastest and restores the densities.
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows) {
   int rc = check_range(e, first, count);
   if (rc) return rc;
@@ -997,19 +998,34 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
       for (int k = 0; k < ns && !dup; ++k) dup = sched[k][0] == chunk && sched[k][1] == lanes;
       if (!dup && ns < 16) sched[ns][0] = chunk, sched[ns][1] = lanes, ++ns;
     }
+  // the fastest whole-range and the fastest blocked configuration
+  int whole_r = best_r, blk_r = 0, blk_chunk = 0, blk_lanes = 1;
+  float whole = 1e30f, blocked = 1e30f;
   for (int i = 0; !rc && i < nr; ++i)
     for (int k = 0; !rc && k < ns; ++k) {
       float ms;
       if ((rc = trial_s(best_c, wrs[i], sched[k][0], sched[k][1], &ms))) break;
-      // a schedule other than the whole range must win by 2%
-      const float bar = (sched[k][0] == 0) ? best : best * 0.98f;
-      if (ms < bar) {
-        best = ms;
-        best_r = wrs[i];
-        best_chunk = sched[k][0];
-        best_lanes = sched[k][1];
+      if (sched[k][0] == 0) {
+        if (ms < whole) whole = ms, whole_r = wrs[i];
+      } else if (ms < blocked) {
+        blocked = ms, blk_r = wrs[i], blk_chunk = sched[k][0], blk_lanes = sched[k][1];
       }
     }
+  best_r = whole_r;
+  // a blocked schedule must win by 2%; when the short trials put the two
+  // within 5% of each other, both are timed again over three times the
+  // iterations before deciding
+  if (!rc && blocked < 1e29f) {
+    if (blocked < whole * 1.05f && whole < blocked * 1.05f) {
+      float tw = 0.f, tb = 0.f;
+      const int it3 = iterations;
+      iterations = 3 * it3;
+      if (!(rc = trial_s(best_c, whole_r, 0, 1, &tw))) rc = trial_s(best_c, blk_r, blk_chunk, blk_lanes, &tb);
+      iterations = it3;
+      whole = tw, blocked = tb;
+    }
+    if (!rc && blocked < whole * 0.98f) best_r = blk_r, best_chunk = blk_chunk, best_lanes = blk_lanes;
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (rc) return rc;
