@@ -1,7 +1,9 @@
 """Build, load and time the plain per-individual cuFFT path
 (``baseline/plain_cufft.cu``): the reference's execution structure with one
 stream, one cuFFT plan and separate kernels per context, individuals spread
-over OpenMP host threads."""
+over OpenMP host threads.  ``kernels="reference"`` runs the reference's own
+compiled kernels (``baseline/ref_kernels.py``) in that structure instead of
+the restated ones."""
 from __future__ import annotations
 
 import ctypes as C
@@ -25,7 +27,7 @@ def build(verbose=False) -> Path:
         return OUT
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
-           "-Xcompiler", "-fPIC,-fopenmp", "-o", str(OUT), str(src), "-lcufft", "-lgomp"]
+           "-Xcompiler", "-fPIC,-fopenmp", "-o", str(OUT), str(src), "-lcufft", "-lgomp", "-ldl"]
     subprocess.check_call(cmd)
     if verbose:
         print(f"built {OUT}")
@@ -39,6 +41,8 @@ def load():
         lib.plain_create.restype = C.c_void_p
         lib.plain_create.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int]
         lib.plain_destroy.argtypes = [C.c_void_p]
+        lib.plain_load_reference_kernels.restype = C.c_int
+        lib.plain_load_reference_kernels.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_char_p)]
         lib.plain_iterate.restype = C.c_int
         lib.plain_iterate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
                                       C.c_float, C.c_int]
@@ -47,13 +51,28 @@ def load():
 
 
 class Plain:
-    def __init__(self, A, nctx=8, device=0):
+    def __init__(self, A, nctx=8, device=0, kernels="restated"):
         self.lib = load()
         A = np.ascontiguousarray(A, dtype=np.float32)
         self.n = A.shape[0]
         self.h = self.lib.plain_create(self.n, A.ctypes.data, int(nctx), int(device))
         if not self.h:
             raise RuntimeError("plain baseline: context creation failed")
+        if kernels == "reference":
+            from baseline import ref_kernels
+            if not ref_kernels.available():
+                self.close()
+                raise RuntimeError("the reference's compiled kernels are not built (baseline/ref_kernels.py)")
+            image = ref_kernels.CUBIN.read_bytes()
+            names = ("normalize", "sub_intensities", "er", "hio", "raar")
+            syms = (C.c_char_p * len(names))(*[ref_kernels.SYMBOLS[k].encode() for k in names])
+            rc = self.lib.plain_load_reference_kernels(self.h, image, syms)
+            if rc:
+                self.close()
+                raise RuntimeError(f"plain baseline: loading the reference's kernels failed ({rc})")
+        elif kernels != "restated":
+            raise ValueError(kernels)
+        self.kernels = kernels
 
     def close(self):
         if self.h:

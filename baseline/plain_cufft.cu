@@ -10,8 +10,16 @@
 // trailing projection, a stream synchronisation and staged D2H copies.  With
 // `copies` == 0 the population stays in device memory and only the kernels
 // and transforms run (the device-resident comparison).
+//
+// Two kernel sets run in that structure: the restatement below, and, after
+// plain_load_reference_kernels, the reference's own compiled kernels
+// (normalize, sub_intensities, apply_support_{er,hio,raar} of
+// gpu_context.cu, built into a cubin from the reference checkout) launched
+// through the CUDA driver, so the reference's real GPU code is timed too.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
+#include <dlfcn.h>
 #include <math.h>
 #include <omp.h>
 #include <stdint.h>
@@ -91,10 +99,26 @@ struct Ctx {
   int* h_S = nullptr;
 };
 
+// The reference's kernels in a loaded module, reached through the driver
+// library at run time (nothing links against it at build time).
+enum RefFn { kNormalize, kSubIntensities, kEr, kHio, kRaar, kRefFns };
+
+struct RefKernels {
+  void* libcuda = nullptr;
+  CUmodule mod = nullptr;
+  CUcontext ctx = nullptr;
+  CUfunction fn[kRefFns] = {};
+  CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, CUstream,
+                     void**, void**) = nullptr;
+  CUresult (*set_current)(CUcontext) = nullptr;
+  CUresult (*unload)(CUmodule) = nullptr;
+};
+
 struct Plain {
   int n = 0, dev = 0;
   float* A = nullptr;
   std::vector<Ctx> ctx;
+  RefKernels ref;
 };
 
 float largest_float_not_above(double t) {
@@ -134,6 +158,11 @@ void plain_destroy(void* h) {
   Plain* p = (Plain*)h;
   if (!p) return;
   cudaSetDevice(p->dev);
+  if (p->ref.mod) {
+    p->ref.set_current(p->ref.ctx);
+    p->ref.unload(p->ref.mod);
+  }
+  if (p->ref.libcuda) dlclose(p->ref.libcuda);
   for (Ctx& c : p->ctx) {
     cufftDestroy(c.plan);
     cudaStreamDestroy(c.st);
@@ -145,6 +174,40 @@ void plain_destroy(void* h) {
   }
   cudaFree(p->A);
   delete p;
+}
+
+// Loads the reference's compiled kernels (a cubin image) into the device's
+// primary context; `symbols` names normalize, sub_intensities,
+// apply_support_er, apply_support_hio and apply_support_raar in that order.
+// Afterwards plain_iterate launches them instead of the restatement.
+// Returns 0 on success.
+int plain_load_reference_kernels(void* h, const void* image, const char* const* symbols) {
+  Plain* p = (Plain*)h;
+  RefKernels& r = p->ref;
+  if (r.mod) return 0;
+  if (cudaSetDevice(p->dev) != cudaSuccess || cudaFree(nullptr) != cudaSuccess) return 1;
+  r.libcuda = dlopen("libcuda.so.1", RTLD_NOW | RTLD_LOCAL);
+  if (!r.libcuda) return 2;
+  auto load = (CUresult(*)(CUmodule*, const void*))dlsym(r.libcuda, "cuModuleLoadData");
+  auto get = (CUresult(*)(CUfunction*, CUmodule, const char*))dlsym(r.libcuda, "cuModuleGetFunction");
+  auto current = (CUresult(*)(CUcontext*))dlsym(r.libcuda, "cuCtxGetCurrent");
+  r.launch = (decltype(r.launch))dlsym(r.libcuda, "cuLaunchKernel");
+  r.set_current = (decltype(r.set_current))dlsym(r.libcuda, "cuCtxSetCurrent");
+  r.unload = (decltype(r.unload))dlsym(r.libcuda, "cuModuleUnload");
+  if (!load || !get || !current || !r.launch || !r.set_current || !r.unload) return 3;
+  if (current(&r.ctx) != CUDA_SUCCESS || !r.ctx) return 4;
+  if (load(&r.mod, image) != CUDA_SUCCESS) {
+    r.mod = nullptr;
+    return 5;
+  }
+  for (int k = 0; k < kRefFns; ++k) {
+    if (get(&r.fn[k], r.mod, symbols[k]) != CUDA_SUCCESS) {
+      r.unload(r.mod);
+      r.mod = nullptr;
+      return 6;
+    }
+  }
+  return 0;
 }
 
 // Runs `iterations` of HIO/RAAR/ER (upd 0/1/2) on `count` individuals.
@@ -161,7 +224,7 @@ int plain_iterate(void* h, float* rho, int32_t* S, int count, int iterations, in
   const float tlo = largest_float_not_above(t);
   const dim3 block(32, 32), grid((n + 31) / 32, (n + 31) / 32);
   int err = 0;
-#pragma omp parallel for schedule(dynamic) num_threads((int)p->ctx.size())
+#pragma omp parallel for schedule(dynamic) num_threads((int)p->ctx.size()) reduction(|| : err)
   for (int irec = 0; irec < count; ++irec) {
     cudaSetDevice(p->dev);
     Ctx& c = p->ctx[omp_get_thread_num()];
@@ -176,13 +239,38 @@ int plain_iterate(void* h, float* rho, int32_t* S, int count, int iterations, in
       d = (float2*)rho + np * irec;
       s = S + np * irec;
     }
-    cudaMemcpyAsync(c.buf, d, np * sizeof(float2), cudaMemcpyDeviceToDevice, c.st);
-    for (int it = 0; it <= iterations; ++it) {
-      cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_INVERSE);
-      k_project<<<grid, block, 0, c.st>>>(d, p->A, n);
-      cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_FORWARD);
-      k_scale<<<grid, block, 0, c.st>>>(d, n);
-      if (it < iterations) k_update<<<grid, block, 0, c.st>>>(d, s, c.buf, beta, n, upd, thi, tlo);
+    if (p->ref.mod) {
+      // GPU_context::HIO / RAAR / ER (gpu_context.cu:778-902) with its kernels
+      const RefKernels& r = p->ref;
+      if (r.set_current(r.ctx) != CUDA_SUCCESS) err = 1;
+      const CUstream st = (CUstream)c.st;
+      float* A = p->A;
+      float b = beta, re = real;
+      int nn = n;
+      void* a_proj[] = {&d, &A, &nn};
+      void* a_norm[] = {&d, &nn};
+      void* a_er[] = {&d, &s, &nn, &re};
+      void* a_upd[] = {&d, &s, &c.buf, &b, &nn, &re};
+      const CUfunction f_upd = r.fn[upd == 0 ? kHio : (upd == 1 ? kRaar : kEr)];
+      void** a_f_upd = upd == 2 ? a_er : a_upd;
+      if (upd != 2) cudaMemcpyAsync(c.buf, d, np * sizeof(float2), cudaMemcpyDeviceToDevice, c.st);
+      for (int it = 0; it <= iterations; ++it) {
+        cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_INVERSE);
+        err |= r.launch(r.fn[kSubIntensities], grid.x, grid.y, 1, 32, 32, 1, 0, st, a_proj, nullptr) != CUDA_SUCCESS;
+        cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_FORWARD);
+        err |= r.launch(r.fn[kNormalize], grid.x, grid.y, 1, 32, 32, 1, 0, st, a_norm, nullptr) != CUDA_SUCCESS;
+        if (it < iterations)
+          err |= r.launch(f_upd, grid.x, grid.y, 1, 32, 32, 1, 0, st, a_f_upd, nullptr) != CUDA_SUCCESS;
+      }
+    } else {
+      cudaMemcpyAsync(c.buf, d, np * sizeof(float2), cudaMemcpyDeviceToDevice, c.st);
+      for (int it = 0; it <= iterations; ++it) {
+        cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_INVERSE);
+        k_project<<<grid, block, 0, c.st>>>(d, p->A, n);
+        cufftExecC2C(c.plan, (cufftComplex*)d, (cufftComplex*)d, CUFFT_FORWARD);
+        k_scale<<<grid, block, 0, c.st>>>(d, n);
+        if (it < iterations) k_update<<<grid, block, 0, c.st>>>(d, s, c.buf, beta, n, upd, thi, tlo);
+      }
     }
     if (copies) {
       cudaMemcpyAsync(c.h_rho, c.rho, np * sizeof(float2), cudaMemcpyDeviceToHost, c.st);

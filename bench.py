@@ -63,6 +63,10 @@ def parse():
                     help="profiling case: two RAAR iterations per pattern side 256..2048")
     ap.add_argument("--profile-memetic", action="store_true",
                     help="profiling case: one memetic generation at 512^2 x 64 through the Solver")
+    ap.add_argument("--profile-plain", default="", choices=["", "restated", "reference"],
+                    help="profiling case: the plain per-individual cuFFT path (restated kernels or the reference's "
+                         "own) at 512^2 x 64, one warm-up iteration and one call of --plain-profile-iters")
+    ap.add_argument("--plain-profile-iters", type=int, default=2)
     ap.add_argument("--pop-sweep", action="store_true", help="iteration rate against population size at 512^2")
     ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
@@ -203,14 +207,15 @@ def cpu_baseline(sample_s: float, threads: int | None = None):
     return cpu_port.time_raar(A, dens, S, BETA, sample_s, threads=threads)
 
 
-def plain_gpu(args, A, dens, S, local, eng):
+def plain_gpu(args, A, dens, S, local, eng, kernels="restated"):
     """The plain per-individual cuFFT path (8 contexts, the reference's
     structure) on the same population, device resident and with the
     reference's staged host copies; and the R-factor both reach from the
-    same start."""
+    same start.  kernels="reference" launches the reference's own compiled
+    kernels in that structure instead of the restated ones."""
     import torch
     from baseline import plain
-    pl = plain.Plain(A, nctx=8, device=local)
+    pl = plain.Plain(A, nctx=8, device=local, kernels=kernels)
     dev = f"cuda:{local}"
     d_rho = torch.from_numpy(dens.view(np.float32).copy()).to(dev)
     d_S = torch.from_numpy(S.copy()).to(dev)
@@ -260,17 +265,20 @@ def plain_gpu(args, A, dens, S, local, eng):
     seq = [(1, 500), (2, 100)]
     f_eng = on_engine(dens, seq)
     f_plain = on_plain(dens, seq)
-    ulp = (dens.view(np.float32) * np.float32(1 + 2 ** -22)).view(np.complex64)
-    f_ulp = on_engine(ulp, seq)
     pl.close()
     final = stats(f_eng, f_plain)
-    final.update({"sequence": "RAAR 500 (beta 0.87) + ER 100",
-                  "engine_vs_1ulp_start_mean_abs_diff": float(abs(f_eng.mean() - f_ulp.mean())),
-                  "engine_vs_1ulp_start_max_abs_diff": float(np.max(np.abs(f_eng - f_ulp)))})
+    final["sequence"] = "RAAR 500 (beta 0.87) + ER 100"
+    if kernels == "restated":
+        ulp = (dens.view(np.float32) * np.float32(1 + 2 ** -22)).view(np.complex64)
+        f_ulp = on_engine(ulp, seq)
+        final.update({"engine_vs_1ulp_start_mean_abs_diff": float(abs(f_eng.mean() - f_ulp.mean())),
+                      "engine_vs_1ulp_start_max_abs_diff": float(np.max(np.abs(f_eng - f_ulp)))})
+    what = {"restated": "per-individual cuFFT C2C pair + projection, /N^2 and update kernels (32x32 blocks) per "
+                        "iteration on 8 streams / OpenMP threads, as the reference's Solver drives GPU_context",
+            "reference": "the reference's own compiled kernels (gpu_context.cu, --use_fast_math, sm_103a cubin) with "
+                         "cuFFT, in the same 8-context structure"}[kernels]
     return {"value": round(value, 1), "unit": "iter*individuals/s",
-            "e2e": round(POP * args.iters / dt_e2e, 1), "contexts": 8,
-            "what": "per-individual cuFFT C2C pair + projection, /N^2 and update kernels (32x32 blocks) per "
-                    "iteration on 8 streams / OpenMP threads, as the reference's Solver drives GPU_context",
+            "e2e": round(POP * args.iters / dt_e2e, 1), "contexts": 8, "kernels": kernels, "what": what,
             "rfactor_after_step": stats(r_eng, r_plain), "rfactor_final": final}
 
 
@@ -601,6 +609,18 @@ def run_engine(args):
             out["plain_gpu"]["fused_over_plain"] = round(value / world / out["plain_gpu"]["value"], 3)
         except Exception as ex:
             out["plain_gpu"] = {"error": str(ex)[:200]}
+        from baseline import ref_kernels
+        if ref_kernels.available():
+            try:
+                rk = plain_gpu(args, A, dens, S, local, eng, kernels="reference")
+                rk["fused_over_reference_kernels"] = round(value / world / rk["value"], 3)
+                rk["e2e_over_reference_kernels_e2e"] = round(out["e2e"]["value"] / world / rk["e2e"], 3)
+                out["reference_gpu_kernels"] = rk
+            except Exception as ex:
+                out["reference_gpu_kernels"] = {"error": str(ex)[:200]}
+        else:
+            out["reference_gpu_kernels"] = {"unavailable": "the reference's kernels were not compiled (its "
+                                                           "checkout was absent where the tree was built)"}
     if rank == 0 and args.batch_patterns > 0:
         try:
             out["batched_sizes"] = batched_sizes(args, local)
@@ -775,6 +795,24 @@ def run_profile_memetic():
                       "sequence": run.algman.sequence(run.generation, area=[1, 1])}))
 
 
+def run_profile_plain(args):
+    """The plain per-individual cuFFT path on the resident population workload
+    (8 contexts), restated kernels or the reference's own compiled ones, for
+    per-kernel ncu launch lists."""
+    import torch
+    from baseline import plain
+    A, dens, S = workload()
+    pl = plain.Plain(A, nctx=8, device=0, kernels=args.profile_plain)
+    d_rho = torch.from_numpy(dens.view(np.float32).copy()).cuda()
+    d_S = torch.from_numpy(S.copy()).cuda()
+    pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, 1, 1, BETA, 0.0, copies=False)
+    pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, args.plain_profile_iters, 1, BETA, 0.0, copies=False)
+    torch.cuda.synchronize()
+    pl.close()
+    print(json.dumps({"profile_case": "plain per-individual path", "kernels": args.profile_plain, "n": N,
+                      "population": POP, "iterations": [1, args.plain_profile_iters]}))
+
+
 def run_pop_sweep(args):
     """Iteration rate against population size at 512^2 (RAAR 100 per call,
     autotuned per population, CUDA events, median of 5 calls)."""
@@ -822,6 +860,9 @@ def main():
         return
     if args.pop_sweep:
         run_pop_sweep(args)
+        return
+    if args.profile_plain:
+        run_profile_plain(args)
         return
     if args.profile_loss:
         run_profile_loss()

@@ -1,7 +1,8 @@
 """The reference's own GPU iteration (TEST INFRASTRUCTURE, never part of the
 engine): the device code of src/gpu/gpu_context.cu, compiled from the
-reference checkout by build_ref_gpu.py into oracle/_ref/ref_gpu_context.cubin,
-loaded through the CUDA driver and driven with cuFFT in the order
+reference checkout by baseline/ref_kernels.py into
+baseline/_build/ref_gpu_context.cubin, loaded through the CUDA driver and
+driven with cuFFT in the order
 GPU_context::HIO / RAAR / ER issue their calls (gpu_context.cu:778-902):
 
     buffer <- density                               (HIO, RAAR: :783-784, :825-826)
@@ -19,19 +20,11 @@ context of the reference's Solver handles its share.
 from __future__ import annotations
 
 import ctypes as C
-from pathlib import Path
 
 import numpy as np
 
-CUBIN = Path(__file__).resolve().parent / "_ref" / "ref_gpu_context.cubin"
-# the kernels' C++ symbols: cufftComplex is float2, FLOAT float, SUPPORTTYPE int
-SYMBOLS = {
-    "normalize": "_Z9normalizeP6float2i",                    # normalize(CUDA_COMPLEX*, int), :65
-    "sub_intensities": "_Z15sub_intensitiesP6float2Pfi",     # :79
-    "er": "_Z16apply_support_erP6float2Piif",                # :519
-    "hio": "_Z17apply_support_hioP6float2PiS0_fif",          # :540
-    "raar": "_Z18apply_support_raarP6float2PiS0_fif",        # :568
-}
+from baseline.ref_kernels import CUBIN, SYMBOLS
+
 CUFFT_C2C, CUFFT_FORWARD, CUFFT_INVERSE = 0x29, -1, 1
 
 

@@ -22,7 +22,7 @@ arithmetic.  Precision policy:
 Parity status: the reference repository carries no golden vectors, fixtures or
 known-answer tests for this path, and its only implementation needs a GPU plus
 cuFFT.  The iteration arithmetic is pinned against that implementation itself:
-``oracle/build_ref_gpu.py`` compiles the device code of ``gpu_context.cu``
+``baseline/ref_kernels.py`` compiles the device code of ``gpu_context.cu``
 from the reference checkout into a cubin, and ``oracle/ref_gpu.py`` drives
 it with cuFFT in ``GPU_context``'s call order; after one HIO / RAAR / ER
 iteration (with and without the positivity gate) this oracle agrees with it

@@ -1,5 +1,5 @@
 """Parity against the reference's own GPU kernels: the device code of its
-src/gpu/gpu_context.cu (oracle/_ref/ref_gpu_context.cubin, compiled from
+src/gpu/gpu_context.cu (baseline/_build/ref_gpu_context.cubin, compiled from
 the reference checkout with the reference's CUDA flags) driven by cuFFT in
 GPU_context::HIO / RAAR / ER's call order (oracle/ref_gpu.py).
 
@@ -23,7 +23,7 @@ from s_spi_spring_gb300 import _lib, synthetic
 pytestmark = pytest.mark.gpu
 
 if not ref_gpu.available():
-    pytest.skip("the reference's GPU kernels are not built (oracle/build_ref_gpu.py needs the reference checkout)",
+    pytest.skip("the reference's GPU kernels are not built (baseline/ref_kernels.py needs the reference checkout)",
                 allow_module_level=True)
 
 
@@ -94,3 +94,28 @@ def test_final_rfactor_matches_reference_kernels():
     e.close()
     print("reference kernels", r_ref.mean(), "engine", r_eng.mean())
     assert abs(r_eng.mean() - r_ref.mean()) < 1e-4
+
+
+@pytest.mark.parametrize("alg,upd,beta,real", [("HIO", 0, 0.9, 0.0), ("RAAR", 1, 0.87, 0.0), ("ER", 2, 0.0, 0.5)])
+def test_baseline_runs_the_reference_kernels(alg, upd, beta, real):
+    """The benchmark's reference-kernel baseline (8 OpenMP contexts, the
+    reference's compiled kernels launched through the driver) gives exactly
+    what one reference context gives: same kernels, same cuFFT plan."""
+    import torch
+    from baseline import plain
+    n, P, iters = 256, 6, 4
+    A, dens, S = case(n, P, 23)
+    r = ref_gpu.RefGPU(n, A)
+    want = r.iterate(dens, S, alg, iters, beta, real)
+    r.close()
+    pl = plain.Plain(A, nctx=3, device=0, kernels="reference")
+    d_rho = torch.from_numpy(dens.view(np.float32).copy()).cuda()
+    d_S = torch.from_numpy(S.copy()).cuda()
+    pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), P, iters, upd, beta, real, copies=False)
+    torch.cuda.synchronize()
+    got_dev = d_rho.cpu().numpy().view(np.complex64).reshape(P, n, n)
+    h_rho, h_S = dens.copy(), S.copy()
+    pl.iterate(h_rho.ctypes.data, h_S.ctypes.data, P, iters, upd, beta, real, copies=True)
+    pl.close()
+    assert np.array_equal(got_dev, want)
+    assert np.array_equal(h_rho, want) and np.array_equal(h_S, S)
