@@ -31,6 +31,18 @@ SYMBOLS = {
     "er": "_Z16apply_support_erP6float2Piif",                # :519
     "hio": "_Z17apply_support_hioP6float2PiS0_fif",          # :540
     "raar": "_Z18apply_support_raarP6float2PiS0_fif",        # :568
+    # shrink-wrap, error metrics and symmetry (oracle/ref_gpu.py only)
+    "get_module": "_Z10get_moduleP6float2i",                          # :6
+    "normalize_shift": "_Z15normalize_shiftP6float2fi",               # :21
+    "normalize_ft_shift": "_Z18normalize_ft_shiftP6float2fi",         # :37
+    "smooth_intensities": "_Z18smooth_intensitiesP6float2fi",         # :199
+    "get_module_sum": "_Z14get_module_sumP6float2Pffi",               # :219
+    "get_error_gpu": "_Z13get_error_gpuP6float2PfiS1_",               # :352
+    "get_real_error_gpu": "_Z18get_real_error_gpuP6float2PifiPf",     # :386
+    "get_max_module": "_Z14get_max_moduleP6float2Pfi",                # :435
+    "cut_support_rel": "_Z11cut_supportP6float2PifPfi",               # :466, threshold x maximum
+    "cut_support_abs": "_Z11cut_supportP6float2Pifi",                 # :484, absolute threshold
+    "multiply_band": "_Z8multiplyP6float2S0_S0_Pffffi",               # :1157
 }
 
 

@@ -12,6 +12,11 @@ GPU_context::HIO / RAAR / ER's call order (oracle/ref_gpu.py).
   phase-gate decision can flip for a pixel, as against the oracle).
 * From the same start, after RAAR 100 + ER 100 the population's mean
   R-factor agrees within 1e-4.
+* Solver::Evaluate's metrics (get_error + get_symmetry) agree within 2e-5
+  (the sums; the reference accumulates them with float atomics) and 1e-4
+  (the real-space error and the symmetry).
+* Shrink-wrap (SW, SWA) gives the reference's supports except for pixels
+  whose filtered modulus ties the cut level within 1e-4.
 """
 import numpy as np
 import pytest
@@ -119,3 +124,69 @@ def test_baseline_runs_the_reference_kernels(alg, upd, beta, real):
     pl.close()
     assert np.array_equal(got_dev, want)
     assert np.array_equal(h_rho, want) and np.array_equal(h_S, S)
+
+
+def object_like(n, count, seed):
+    """A pattern, and densities after a few engine ER iterations (object-like
+    moduli, so that metrics and cuts are taken on realistic inputs)."""
+    A, dens, S = case(n, count, seed)
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, dens, S)
+    e.hio(0, count, 10, 0.9, 0.0)
+    e.er(0, count, 3, 0.0)
+    cur, _ = e.download(0, count)
+    return A, cur, S, e
+
+
+@pytest.mark.parametrize("n", [64, 256, 512])
+@pytest.mark.parametrize("reality", [0.0, 0.5])
+def test_evaluate_matches_reference_kernels(n, reality):
+    A, cur, S, e = object_like(n, 3, n + 5)
+    e.upload(0, cur, S)
+    got = e.evaluate(0, 3, reality, 0.25)
+    e.close()
+    r = ref_gpu.RefGPU(n, A)
+    want = r.evaluate(cur, S, reality, 0.25)
+    r.close()
+    for i in range(3):
+        print(n, reality, i, {k: (got[i][k], want[i][k]) for k in want[i]})
+        for k, tol in (("error_fourier", 2e-5), ("modulesum", 2e-5), ("complexsum", 2e-5), ("error", 2e-5),
+                       ("error_real", 1e-4), ("symmetry", 1e-4)):
+            assert abs(got[i][k] - want[i][k]) <= tol * abs(want[i][k]) + 1e-7, (k, i, got[i][k], want[i][k])
+        assert abs(got[i]["reality"] - want[i]["reality"]) <= 2e-5
+
+
+def cut_agrees(got, want, m, cut):
+    """Supports equal except where the reference's filtered modulus ties
+    the cut level within 1e-4 relative."""
+    diff = got != want
+    near = np.abs(m - cut) <= 1e-4 * max(float(cut), 1e-30)
+    return int(diff.sum()), bool(np.all(near[diff]))
+
+
+@pytest.mark.parametrize("n", [64, 256, 512])
+def test_shrinkwrap_matches_reference_kernels(n):
+    A, cur, S, e = object_like(n, 2, n + 7)
+    r = ref_gpu.RefGPU(n, A)
+    for sigma, thr in ((3.0, 0.1), (1.5, 0.05)):
+        e.upload(0, cur, S)
+        e.sw(0, 2, sigma, thr, 0.0)
+        gd, gs = e.download(0, 2)
+        assert np.array_equal(gd, cur)
+        ws, wm, wc = r.sw(cur, S, sigma, thr)
+        for i in range(2):
+            ndiff, ok = cut_agrees(gs[i], ws[i], wm[i], wc[i])
+            print("SW", n, sigma, thr, i, "support", int(ws[i].sum()), "differ", ndiff)
+            assert ok, (n, sigma, thr, i, ndiff)
+    for sigma, k in ((2.5, 500), (1.0, 2000), (2.0, 1)):
+        e.upload(0, cur, S)
+        e.swa(0, 2, sigma, k, 0.0)
+        _, gs = e.download(0, 2)
+        ws, wm, wc = r.swa(cur, S, sigma, k)
+        for i in range(2):
+            ndiff, ok = cut_agrees(gs[i], ws[i], wm[i], wc[i])
+            print("SWA", n, sigma, k, i, "support", int(ws[i].sum()), int(gs[i].sum()), "differ", ndiff)
+            assert ok, (n, sigma, k, i, ndiff)
+    r.close()
+    e.close()
