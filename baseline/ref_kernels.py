@@ -43,6 +43,13 @@ SYMBOLS = {
     "cut_support_rel": "_Z11cut_supportP6float2PifPfi",               # :466, threshold x maximum
     "cut_support_abs": "_Z11cut_supportP6float2Pifi",                 # :484, absolute threshold
     "multiply_band": "_Z8multiplyP6float2S0_S0_Pffffi",               # :1157
+    "shift": "_Z5shiftP6float2S0_PiS1_iifbi",                         # :1329
+    "add_module": "_Z10add_moduleP6float2Pfi",                        # :114
+    "add_complex": "_Z3addP6float2S0_i",                              # :125
+    "add_support": "_Z3addPiS_i",                                     # :186
+    "cross_density": "_Z13cross_densityP6float2S0_S0_S0_S0_S0_PiPfS2_iiiiiiifffb",      # :1699
+    "cross_density_real": "_Z18cross_density_realP6float2S0_S0_S0_S0_PiPfS2_iiiiiiifffb",  # :1799
+    "cross_support": "_Z13cross_supportPiS_S_S_i",                    # :1856
 }
 
 

@@ -17,6 +17,13 @@ GPU_context::HIO / RAAR / ER's call order (oracle/ref_gpu.py).
   (the real-space error and the symmetry).
 * Shrink-wrap (SW, SWA) gives the reference's supports except for pixels
   whose filtered modulus ties the cut level within 1e-4.
+* Alignment (Solver::Reshift) finds the reference's shifts and flips: the
+  supports are identical and the densities agree within 1e-5.
+* The average (Solver::GetAverage) is bit-identical; the average module
+  (Solver::GetAverageModule) agrees within 1e-5, and the
+  crossover's children (Solver::Crossover on the same draws) agree except on
+  at most 0.5% of the pixels, where a crossmap cell boundary passes within
+  float rounding of a pixel (the cell map goes through cos / sin).
 """
 import numpy as np
 import pytest
@@ -190,3 +197,100 @@ def test_shrinkwrap_matches_reference_kernels(n):
             assert ok, (n, sigma, k, i, ndiff)
     r.close()
     e.close()
+
+
+def shifted_copies(n, P, seed):
+    """Shifted, twin-flipped, phase-rotated noisy copies of one object, each
+    with its own support (unambiguous correlation peaks)."""
+    rng = np.random.default_rng(seed)
+    I, obj, supp = synthetic.polygon_pattern(seed=seed + 1, n=n, diameter=n * 0.3, photons=1e9, stop_radius=2)
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    rhos, Ss = [], []
+    for k in range(P):
+        sx, sy = rng.integers(-n // 12, n // 12, 2)
+        r = np.roll(obj, (sy, sx), axis=(0, 1)) * np.exp(1j * rng.uniform(-3, 3))
+        sp = np.roll(supp, (sy, sx), axis=(0, 1))
+        if k % 3 == 2:
+            r = np.conj(r[::-1, ::-1])
+            sp = sp[::-1, ::-1]
+        r = r + 0.02 * (rng.standard_normal(r.shape) + 1j * rng.standard_normal(r.shape)) * (sp > 0)
+        rhos.append(r.astype(np.complex64))
+        Ss.append(np.ascontiguousarray(sp, dtype=np.int32))
+    return A, np.stack(rhos), np.stack(Ss)
+
+
+@pytest.mark.parametrize("n,minr,maxr", [(128, 0.0, 2.0), (256, 0.0, 2.0), (256, 0.05, 0.8)])
+def test_reshift_matches_reference_kernels(n, minr, maxr):
+    P = 6
+    A, rhos, Ss = shifted_copies(n, P, seed=n + 1)
+    ref = rhos[0].copy()
+    r = ref_gpu.RefGPU(n, A)
+    wd, ws, shifts = r.reshift(rhos, Ss, ref, minr, maxr)
+    r.close()
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, rhos, Ss)
+    e.reshift(0, P, -1, ref, minr, maxr)
+    gd, gs = e.download(0, P)
+    e.close()
+    print(n, minr, maxr, shifts)
+    assert any(f for *_, f in shifts) and not all(f for *_, f in shifts)
+    for i in range(P):
+        assert np.array_equal(gs[i], ws[i]), (i, shifts[i])
+        d = rel(gd[i], wd[i])
+        print(i, d)
+        assert d < 1e-5, (i, d)
+
+
+@pytest.mark.parametrize("crossft,use_average,update_support,seed",
+                         [(1.0, 0.0, True, 17), (0.0, 0.0, True, 18), (0.5, 0.5, False, 19), (1.0, -0.5, True, 20)])
+def test_crossover_matches_reference_kernels(crossft, use_average, update_support, seed):
+    n, P = 128, 6
+    A, rhos, Ss = shifted_copies(n, P, seed=seed)
+    errors = np.random.default_rng(seed).uniform(0.1, 0.9, P).astype(np.float32)
+    best = int(np.argmin(errors))
+    avg_d, avg_s = o.get_average(list(rhos), list(Ss), errors, 0.8)
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.seed(seed)
+    e.reserve(2 * P + 2)
+    e.upload(0, rhos, Ss)
+    e.upload(P, rhos[best][None], Ss[best][None])
+    e.upload(P + 1, avg_d[None], avg_s[None])
+    got_mod = e.average_module(0, P, errors, True, 0.66)
+    e.crossover(0, P, errors, P, P + 1, P + 2, 0.6, 0.4, 1.0, crossft, False, use_average, update_support,
+                0.0, 0.0, 2.0)
+    gd, gs = e.download(P + 2, P)
+    e.close()
+    r = ref_gpu.RefGPU(n, A)
+    avg_mod = r.average_module(rhos, errors, True, 0.66)
+    assert rel(got_mod, avg_mod) < 1e-5, rel(got_mod, avg_mod)
+    draws = o.draw_crossover(o.ContextRNG(seed), P, o.sorted_indexes(errors), o.suppdim_of(Ss[best], n), n,
+                             0.6, 1.0, crossft)
+    want = r.crossover(rhos, Ss, rhos[best], avg_d, avg_mod, draws, 0.4, use_average, False, update_support)
+    r.close()
+    for i, (rd, rs) in enumerate(want):
+        smis = np.mean(gs[i] != rs)
+        bad = np.abs(gd[i] - rd) > 1e-4 * np.abs(rd).max()
+        print(i, "crossft", draws[i].crossft, "support mismatch", smis, "density mismatch", bad.mean())
+        assert smis <= 5e-3, (i, smis)
+        assert bad.mean() <= 5e-3, (i, bad.mean())
+
+
+@pytest.mark.parametrize("fraction", [1.0, 0.8, 0.34, 0.0])
+def test_average_bit_identical_to_reference_kernels(fraction):
+    n, P = 128, 7
+    A, rhos, Ss = shifted_copies(n, P, seed=29)
+    errors = np.random.default_rng(2).uniform(0.1, 0.9, P).astype(np.float32)
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, rhos, Ss)
+    e.reserve(P + 1)
+    e.average(0, P, errors, fraction, P)
+    gd, gs = e.download(P, 1)
+    e.close()
+    r = ref_gpu.RefGPU(n, A)
+    wd, ws = r.average(rhos, Ss, errors, fraction)
+    r.close()
+    assert np.array_equal(gs[0], ws)
+    assert np.array_equal(gd[0].view(np.uint32), wd.view(np.uint32))
