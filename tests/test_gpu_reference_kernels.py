@@ -19,6 +19,10 @@ GPU_context::HIO / RAAR / ER's call order (oracle/ref_gpu.py).
   whose filtered modulus ties the cut level within 1e-4.
 * Alignment (Solver::Reshift) finds the reference's shifts and flips: the
   supports are identical and the densities agree within 1e-5.
+* The CPU-sized single-reconstruction workload (HIO 200 with shrink-wrap
+  every 20 iterations, then ER 50) reaches the same noise-limited R-factor
+  through the engine and through the reference's kernels: population means
+  within 1.5e-3 (the run is chaotic, so single runs are not compared).
 * The average (Solver::GetAverage) is bit-identical; the average module
   (Solver::GetAverageModule) agrees within 1e-5, and the
   crossover's children (Solver::Crossover on the same draws) agree except on
@@ -294,3 +298,40 @@ def test_average_bit_identical_to_reference_kernels(fraction):
     r.close()
     assert np.array_equal(gs[0], ws)
     assert np.array_equal(gd[0].view(np.uint32), wd.view(np.uint32))
+
+
+def test_single_reconstruction_workload_matches_reference_kernels():
+    """128 x 128 disc object with a smooth phase, 1e6 photons, 5 x 5 beamstop;
+    HIO 200 at beta 0.9 with shrink-wrap every 20 iterations (sigma 3 ->
+    1.5, threshold 0.1), then ER 50; from the same six random starts through
+    the engine and through Solver-equivalent calls of the reference's own
+    kernels (HIO, SW and ER calls with host round trips, as the Solver makes
+    them)."""
+    n, beta = 128, 0.9
+    sig = [3.0 - 1.5 * k / 9 for k in range(10)]
+    r_eng, r_ref = [], []
+    for seed in (0, 1, 2):
+        I, _, _ = synthetic.disc_pattern(seed=seed, n=n, radius=20, photons=1e6, beamstop=5)
+        A = _lib.prepare_pattern(I, (-1, -1), True)
+        dens, S = synthetic.start_population(n, 2, 30, seed=seed + 50)
+        e = _lib.Engine(n, 0)
+        e.set_amplitudes(A)
+        e.upload(0, dens, S)
+        for k in range(10):
+            e.hio(0, 2, 20, beta, 0.0)
+            e.sw(0, 2, sig[k], 0.1, 0.0)
+        e.er(0, 2, 50, 0.0)
+        r_eng += [m["error_fourier"] for m in e.evaluate(0, 2, 0.0, 0.0)]
+        e.close()
+        r = ref_gpu.RefGPU(n, A)
+        d, sp = dens.copy(), S.copy()
+        for k in range(10):
+            d = r.iterate(d, sp, "HIO", 20, beta, 0.0)
+            sp = r.sw(d, sp, sig[k], 0.1)[0]
+        d = r.iterate(d, sp, "ER", 50, 0.0, 0.0)
+        r_ref += [m["error_fourier"] for m in r.evaluate(d, sp, 0.0, 0.0)]
+        r.close()
+    r_eng, r_ref = np.array(r_eng), np.array(r_ref)
+    print("engine", r_eng, "reference kernels", r_ref, "means", r_eng.mean(), r_ref.mean())
+    assert np.all(r_eng < 0.13) and np.all(r_ref < 0.13)
+    assert abs(r_eng.mean() - r_ref.mean()) < 1.5e-3
