@@ -56,6 +56,8 @@ def parse():
                     help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
     ap.add_argument("--batch-patterns", type=int, default=256,
                     help="patterns of uneven sizes in the graph-captured batch (0: skip)")
+    ap.add_argument("--batch-tune-iters", type=int, default=2,
+                    help="iterations per autotuning trial of each size in the batch")
     ap.add_argument("--large", type=int, default=1, help="time the 2048^2 x 128 population (0: skip)")
     ap.add_argument("--refine", type=int, default=1, help="time the gradient-refinement epoch (0: skip)")
     ap.add_argument("--profile-loss", action="store_true", help="profiling case: one loss + gradient at 512^2 x 64")
@@ -341,7 +343,9 @@ def batched_sizes(args, local):
         pats.append(I)
     b = PatternBatch(pats, population=16, device=local)
     b.initialize()
-    tuned = b.autotune(iterations=2)
+    t0 = time.perf_counter()
+    tuned = b.autotune(iterations=args.batch_tune_iters)
+    tune_s = time.perf_counter() - t0
     hio, er = 20, 10
     b.capture(hio, 0.9, er)
     stream = torch.cuda.ExternalStream(b.stream, device=f"cuda:{local}")
@@ -363,7 +367,8 @@ def batched_sizes(args, local):
            "px_iter_per_s": round(b.pixels_per_iteration() * (hio + er) / (ms / 1e3), 1),
            "iter_ind_per_s": round(b.individuals() * (hio + er) / (ms / 1e3), 1),
            "graph": "one CUDA graph launch per sweep (all sizes)",
-           "tuned": {int(n): v for n, v in tuned.items()},
+           "tuned": {int(n): v for n, v in tuned.items()}, "tune_iterations": args.batch_tune_iters,
+           "tune_s": round(tune_s, 1),
            "rfactor_median": round(float(np.median(rf)), 5)}
     b.close()
     return out
