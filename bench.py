@@ -203,10 +203,18 @@ def peaks():
 
 def cpu_baseline(sample_s: float, threads: int | None = None):
     """The CPU restatement of the path timed on the host cores (bounded sample
-    of the same workload: a few individuals, a few RAAR iterations)."""
+    of the same workload: a few individuals, a few RAAR iterations): the
+    C/OpenMP port, and as a second figure the complex64 scipy.fft
+    restatement over all cores."""
     from oracle import cpu_port
     A, dens, S = workload()
-    return cpu_port.time_raar(A, dens, S, BETA, sample_s, threads=threads)
+    out = cpu_port.time_raar(A, dens, S, BETA, sample_s, threads=threads)
+    try:
+        from oracle import scipy_port
+        out["scipy_fft"] = scipy_port.time_raar(A, dens, S, BETA, sample_s=max(3.0, sample_s * 2 / 3))
+    except Exception as ex:  # scipy is optional on the host
+        out["scipy_fft"] = {"error": str(ex)[:200]}
+    return out
 
 
 def plain_gpu(args, A, dens, S, local, eng, kernels="restated"):
