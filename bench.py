@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--batch-tune-iters", type=int, default=2,
                     help="iterations per autotuning trial of each size in the batch")
     ap.add_argument("--large", type=int, default=1, help="time the 2048^2 x 128 population (0: skip)")
+    ap.add_argument("--large-tune-iters", type=int, default=2,
+                    help="iterations per autotuning trial of the 2048^2 x 128 population")
     ap.add_argument("--refine", type=int, default=1, help="time the gradient-refinement epoch (0: skip)")
     ap.add_argument("--profile-loss", action="store_true", help="profiling case: one loss + gradient at 512^2 x 64")
     ap.add_argument("--profile-sizes", action="store_true",
@@ -457,7 +459,7 @@ def large_population(args, local):
     eng.reserve(P)
     eng.seed(42)
     eng.initialize_pop(0, P, 600, (120.0, 540.0), (2, 8), (0.5, 0.5), (0.5, 1.5), 0.0)
-    tiles = eng.autotune(0, P, 2)
+    tiles = eng.autotune(0, P, args.large_tune_iters)
     sched = eng.schedule()
     eng.raar(0, P, 1, BETA, 0.0)
     eng.synchronize()
@@ -477,7 +479,7 @@ def large_population(args, local):
                         "1e9 photons, 25% of pixels masked", "iterations": iters,
             "ms_per_iteration": round(ms / iters, 3), "iter_ind_per_s": round(P * iters / (ms / 1e3), 1),
             "alg_gbps": round(alg / (ms / 1e3) / 1e9, 1), "frac": round(alg / (ms / 1e3) / 1e9 / peak, 4),
-            "device_state_gb": round(P * n * n * 32 / 1e9, 1), "tiles": list(tiles), "schedule": list(sched),
+            "device_state_gb": round(P * n * n * 32 / 1e9, 1), "tiles": list(tiles), "schedule": list(sched), "tune_iterations": args.large_tune_iters,
             "rfactor_median": round(float(np.median([x["error_fourier"] for x in m])), 5)}
 
 
