@@ -7,10 +7,8 @@ the restated ones."""
 from __future__ import annotations
 
 import ctypes as C
-import os
 import shutil
 import subprocess
-import time
 from pathlib import Path
 
 import numpy as np
