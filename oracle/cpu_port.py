@@ -4,7 +4,6 @@ from __future__ import annotations
 
 import ctypes as C
 import math
-import os
 import time
 
 import numpy as np
