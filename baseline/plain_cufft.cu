@@ -99,7 +99,7 @@ struct Ctx {
   int* h_S = nullptr;
 };
 
-// The reference's kernels in a loaded module, reached through the driver
+// The reference's kernels in a loaded module, reached through the CUDA driver
 // library at run time (nothing links against it at build time).
 enum RefFn { kNormalize, kSubIntensities, kEr, kHio, kRaar, kRefFns };
 

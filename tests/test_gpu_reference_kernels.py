@@ -115,7 +115,7 @@ def test_final_rfactor_matches_reference_kernels():
 @pytest.mark.parametrize("alg,upd,beta,real", [("HIO", 0, 0.9, 0.0), ("RAAR", 1, 0.87, 0.0), ("ER", 2, 0.0, 0.5)])
 def test_baseline_runs_the_reference_kernels(alg, upd, beta, real):
     """The benchmark's reference-kernel baseline (8 OpenMP contexts, the
-    reference's compiled kernels launched through the driver) gives exactly
+    reference's compiled kernels launched through the CUDA driver) gives exactly
     what one reference context gives: same kernels, same cuFFT plan."""
     import torch
     from baseline import plain
