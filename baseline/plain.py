@@ -44,6 +44,8 @@ def load():
         lib.plain_iterate.restype = C.c_int
         lib.plain_iterate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
                                       C.c_float, C.c_int]
+        lib.plain_last_ms.restype = C.c_double
+        lib.plain_last_ms.argtypes = [C.c_void_p]
         _lib = lib
     return _lib
 
@@ -82,3 +84,8 @@ class Plain:
                                     float(real), int(bool(copies)))
         if rc:
             raise RuntimeError("plain baseline: CUDA error")
+
+    def last_ms(self) -> float:
+        """Device time of the last iterate() call (CUDA events on the
+        context streams), in milliseconds."""
+        return float(self.lib.plain_last_ms(self.h))

@@ -91,6 +91,8 @@ __global__ void k_update(float2* d, const int* S, float2* buf, float beta, int n
 
 struct Ctx {
   cudaStream_t st = nullptr;
+  cudaEvent_t end = nullptr;  // recorded after the context's last individual of a call
+  int used = 0;
   cufftHandle plan = 0;
   float2* rho = nullptr;  // working density (copies mode)
   int* S = nullptr;
@@ -117,6 +119,8 @@ struct RefKernels {
 struct Plain {
   int n = 0, dev = 0;
   float* A = nullptr;
+  cudaEvent_t begin = nullptr;  // recorded at the start of a call; every context stream waits on it
+  double last_ms = -1.0;        // device time of the last call: begin to the latest context end
   std::vector<Ctx> ctx;
   RefKernels ref;
 };
@@ -149,7 +153,9 @@ void* plain_create(int n, const float* amp, int nctx, int device) {
     cudaMalloc(&c.buf, np * sizeof(float2));
     cudaMallocHost(&c.h_rho, np * sizeof(float2));
     cudaMallocHost(&c.h_S, np * sizeof(int));
+    cudaEventCreate(&c.end);
   }
+  cudaEventCreate(&p->begin);
   if (cudaDeviceSynchronize() != cudaSuccess) return nullptr;
   return p;
 }
@@ -171,7 +177,9 @@ void plain_destroy(void* h) {
     cudaFree(c.buf);
     cudaFreeHost(c.h_rho);
     cudaFreeHost(c.h_S);
+    cudaEventDestroy(c.end);
   }
+  cudaEventDestroy(p->begin);
   cudaFree(p->A);
   delete p;
 }
@@ -224,6 +232,14 @@ int plain_iterate(void* h, float* rho, int32_t* S, int count, int iterations, in
   const float tlo = largest_float_not_above(t);
   const dim3 block(32, 32), grid((n + 31) / 32, (n + 31) / 32);
   int err = 0;
+  // device-side timing of the call: every context stream starts after
+  // `begin`; each context records `end` after its last individual
+  if (cudaSetDevice(p->dev) != cudaSuccess) return 1;
+  if (cudaEventRecord(p->begin, p->ctx[0].st) != cudaSuccess) return 1;
+  for (Ctx& c : p->ctx) {
+    c.used = 0;
+    if (cudaStreamWaitEvent(c.st, p->begin, 0) != cudaSuccess) return 1;
+  }
 #pragma omp parallel for schedule(dynamic) num_threads((int)p->ctx.size()) reduction(|| : err)
   for (int irec = 0; irec < count; ++irec) {
     cudaSetDevice(p->dev);
@@ -276,13 +292,24 @@ int plain_iterate(void* h, float* rho, int32_t* S, int count, int iterations, in
       cudaMemcpyAsync(c.h_rho, c.rho, np * sizeof(float2), cudaMemcpyDeviceToHost, c.st);
       cudaMemcpyAsync(c.h_S, c.S, np * sizeof(int), cudaMemcpyDeviceToHost, c.st);
     }
+    if (cudaEventRecord(c.end, c.st) != cudaSuccess) err = 1;
+    c.used = 1;
     if (cudaStreamSynchronize(c.st) != cudaSuccess) err = 1;
     if (copies) {
       memcpy(rho + 2 * np * irec, c.h_rho, np * sizeof(float2));
       memcpy(S + np * irec, c.h_S, np * sizeof(int));
     }
   }
+  p->last_ms = -1.0;
+  for (const Ctx& c : p->ctx) {
+    float ms = 0.f;
+    if (c.used && cudaEventElapsedTime(&ms, p->begin, c.end) == cudaSuccess && ms > p->last_ms) p->last_ms = ms;
+  }
   return err;
 }
+
+// Device time of the last plain_iterate call in milliseconds (CUDA events:
+// from the call's start to the last context's end), -1 if unavailable.
+double plain_last_ms(void* h) { return h ? ((Plain*)h)->last_ms : -1.0; }
 
 }  // extern "C"

@@ -23,7 +23,10 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 CUBIN = HERE / "_build" / "ref_gpu_context.cubin"
-DEFAULT_REF = Path("/root/reference")
+sys.path.insert(0, str(HERE.parent))
+from oracle.refroot import reference_root  # noqa: E402
+
+DEFAULT_REF = reference_root()
 # the kernels' C++ symbols: cufftComplex is float2, FLOAT float, SUPPORTTYPE int
 SYMBOLS = {
     "normalize": "_Z9normalizeP6float2i",                    # normalize(CUDA_COMPLEX*, int), gpu_context.cu:65

@@ -35,9 +35,18 @@ N = 512
 POP = 64
 BETA = 0.87
 B_PER_PIXEL_ITER = 24  # rho read+write 16 B, amplitude 4 B, support 4 B
-# DRAM bytes of one iteration (column pass + row pass) at 512^2 x 64, from
-# the committed ncu captures: 135.3 + 78.5 + 335.6 + 208.2 MB
-ITER_DRAM_BYTES = 757_600_000
+# DRAM bytes of one population iteration (column pass + row pass) at
+# 512^2 x 64 per iteration configuration (col tile, row tile code, chunk,
+# lanes), from ncu captures (dram__bytes_read.sum + dram__bytes_write.sum) of
+# the same tiles and schedule:
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum \
+#       --clock-control none python bench.py --profile-iters 20 --tiles=C,R --schedule=K,L
+# summed over one column and one row launch of every lane.  A configuration
+# without a capture reports no traffic.
+ITER_DRAM_BYTES = {
+    (8, 104, 0, 1): 757_700_000,   # 135.3 + 78.4 + 335.6 + 208.4 MB, one whole-range lane
+    (8, 104, 32, 2): 634_000_000,  # 2 x (68.2 + 8.9 + 167.8 + 72.1) MB, two 32-individual lanes
+}
 E2E_BLOCKS = 2  # population blocks of the host-buffer call (measured best of 1-16)
 
 
@@ -51,7 +60,7 @@ def parse():
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--plain-steps", type=int, default=5)
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling case: set up the workload, run one RAAR call of this many iterations, exit")
     ap.add_argument("--batch-patterns", type=int, default=256,
@@ -108,10 +117,20 @@ def whole_job_rate(units_per_rank_step: float, world: int, ms_step: float) -> fl
     return units_per_rank_step * world / (ms_step / 1e3)
 
 
-def workload(seed=1):
-    from s_spi_spring_gb300 import _lib, synthetic
+def workload(seed=1, encoder="engine"):
+    """The benchmark's pattern (encoded amplitudes) and starting population.
+    encoder="oracle" encodes with the oracle's restatement of the reference's
+    Solver::prepare / set_boundaries instead of the engine library, so that
+    the CPU reference arm loads no product library (the two encodings are
+    bit-identical, tests/test_reference_pin.py)."""
+    from s_spi_spring_gb300 import synthetic
     I, _, _ = synthetic.polygon_pattern(seed=seed, n=N, diameter=120.0, photons=1e7, stop_radius=8, gap=4, stripes=2)
-    A = _lib.prepare_pattern(I, (-1, -1), True)
+    if encoder == "oracle":
+        from oracle import spring_oracle
+        A = spring_oracle.prepare_pattern(I, (-1, -1), True).astype(np.float32)
+    else:
+        from s_spi_spring_gb300 import _lib
+        A = _lib.prepare_pattern(I, (-1, -1), True)
     dens, S = synthetic.start_population(N, POP, 70.0, seed=seed + 1)
     return A, dens, S
 
@@ -231,21 +250,27 @@ def plain_gpu(args, A, dens, S, local, eng, kernels="restated"):
     dev = f"cuda:{local}"
     d_rho = torch.from_numpy(dens.view(np.float32).copy()).to(dev)
     d_S = torch.from_numpy(S.copy()).to(dev)
-    pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, 5, 1, BETA, 0.0, copies=False)
+    for _ in range(3):  # warm-up steps
+        pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, 5, 1, BETA, 0.0, copies=False)
     torch.cuda.synchronize()
     d_rho.copy_(torch.from_numpy(dens.view(np.float32).copy()).to(dev))
-    t0 = time.perf_counter()
-    for _ in range(args.plain_steps):
-        pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, args.iters, 1, BETA, 0.0, copies=False)
     torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    value = args.plain_steps * POP * args.iters / dt
+    # each step timed on the device: CUDA events on the context streams
+    # (from the call's start to the last context's end); the population
+    # (192 MiB) exceeds L2 between steps
+    steps_ms = []
+    with ClockSampler(local) as clk:
+        clk.mark_start()
+        for _ in range(args.plain_steps):
+            pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), POP, args.iters, 1, BETA, 0.0, copies=False)
+            steps_ms.append(pl.last_ms())
+        clk.mark_end()
+    value = POP * args.iters / (statistics.median(steps_ms) / 1e3)
     # R-factor after one step from the original start, evaluated by the engine
     h_rho = dens.copy()
     h_S = S.copy()
-    t0 = time.perf_counter()
     pl.iterate(h_rho.ctypes.data, h_S.ctypes.data, POP, args.iters, 1, BETA, 0.0, copies=True)
-    dt_e2e = time.perf_counter() - t0
+    dt_e2e = pl.last_ms() / 1e3
 
     def rfactors(d):
         eng.upload(0, d, S)
@@ -290,6 +315,8 @@ def plain_gpu(args, A, dens, S, local, eng, kernels="restated"):
             "reference": "the reference's own compiled kernels (gpu_context.cu, --use_fast_math, sm_103a cubin) with "
                          "cuFFT, in the same 8-context structure"}[kernels]
     return {"value": round(value, 1), "unit": "iter*individuals/s",
+            "timing": f"CUDA events, median of {args.plain_steps} steps of {args.iters} iterations",
+            "ms_per_step": [round(x, 3) for x in steps_ms], "clocks": clk.summary(),
             "e2e": round(POP * args.iters / dt_e2e, 1), "contexts": 8, "kernels": kernels, "what": what,
             "rfactor_after_step": stats(r_eng, r_plain), "rfactor_final": final}
 
@@ -579,6 +606,13 @@ def run_engine(args):
         e1.synchronize()
         return max_over_ranks(e0.elapsed_time(e1) / args.steps, world, f"cuda:{local}")
 
+    key = (tiles[0], tiles[1], sched[0], sched[1])
+    traffic = ITER_DRAM_BYTES.get(key)
+    traffic_source = (f"ncu dram bytes of one column and one row launch per lane, captured with tiles "
+                      f"{tiles[0]},{tiles[1]} and schedule {sched[0]},{sched[1]} (the timed configuration)"
+                      if traffic else f"no ncu capture of tiles {tiles[0]},{tiles[1]} / schedule "
+                                      f"{sched[0]},{sched[1]}")
+
     e2e_ms = e2e_time(e2e_pipelined)
     e2e_value = units_per_step * world / (e2e_ms / 1e3)
     e2e_serial_value = units_per_step * world / (e2e_time(e2e_serial) / 1e3)
@@ -605,15 +639,13 @@ def run_engine(args):
                 "call": f"spe_iterate_host (pinned host buffers, {E2E_BLOCKS} blocks on two streams)",
                 "serial_upload_iterate_download": round(e2e_serial_value, 1)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": ITER_DRAM_BYTES,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one column pass and "
-                                       "one row pass (profiles/k_cols_project_raar512_pop64.md, "
-                                       "profiles/k_rows_iterate_raar512_pop64.md)",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "traffic_source": traffic_source,
                      "kernel": "fused iteration (column pass + row pass), per iteration",
                      "alg_bytes_per_launch": alg_bytes, "ms_per_iteration": round(t_iter_ms, 5),
                      # the DRAM rate the measured traffic implies at this iteration time
-                     "traffic_gbps": round(ITER_DRAM_BYTES / (t_iter_ms / 1e3) / 1e9, 1),
-                     "traffic_frac": round(ITER_DRAM_BYTES / (t_iter_ms / 1e3) / 1e9 / peak, 4),
+                     "traffic_gbps": round(traffic / (t_iter_ms / 1e3) / 1e9, 1) if traffic else None,
+                     "traffic_frac": round(traffic / (t_iter_ms / 1e3) / 1e9 / peak, 4) if traffic else None,
                      "peak_source": peak_kind},
         "gpu_launches": args.steps * (2 * args.iters + 3) * (-(-POP // sched[0]) if sched[0] > 0 else 1),
         "clocks": clocks.summary(),
@@ -674,7 +706,7 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle import cpu_port
-    A, dens, S = workload()
+    A, dens, S = workload(encoder="oracle")
     per = []
     info = None
     for i in range(args.warmup + args.steps):

@@ -382,13 +382,18 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
  * arrays the caller owns: density (count*n*n complex64, updated in place),
  * support (count*n*n int32), amplitudes (n*n float, the output of
  * spe_prepare_pattern); algorithm is SPE_OP_HIO, SPE_OP_RAAR or SPE_OP_ER;
- * work is queued on cuda_stream (a cudaStream_t, NULL: the legacy stream).
- * The scratch lives in a 16 MiB file-scope device array that every GPU
- * using the library keeps until exit; calls needing more (count*n*n*8 bytes)
- * are rejected with SPE_ERR_INVALID.  The first call on a device sets up
- * that array's address and the twiddle tables (synchronously), so make it
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU (e.g. on two streams) race.  No memory is allocated. */
+ * work is queued on cuda_stream (a cudaStream_t of the current device,
+ * NULL: the legacy stream; a stream of another device is rejected with
+ * SPE_ERR_INVALID).  The scratch lives in a 16 MiB file-scope device array
+ * that every GPU running this entry point keeps until exit; calls needing
+ * more (count*n*n*8 bytes) are rejected with SPE_ERR_INVALID.  The first
+ * call on a device loads the library's device code (CUDA loads modules
+ * lazily), which places the 16 MiB array and the code in device memory, and
+ * sets up the array's address and the twiddle tables, waiting for the
+ * device; so make that first call during start-up, before reserving the
+ * device and before any stream capture.  Later calls allocate nothing.  All
+ * calls share the array: calls that overlap on the GPU (e.g. on two
+ * streams) race. */
 int spe_iterate_noalloc(int n, void* density, const int32_t* support, const float* amplitudes, int count,
                         int algorithm, int iterations, float beta, float reality, void* cuda_stream);
 

@@ -15,7 +15,10 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref" / "libref_driver.so"
-DEFAULT_REF = Path("/root/reference")
+sys.path.insert(0, str(HERE.parent))
+from oracle.refroot import reference_root  # noqa: E402
+
+DEFAULT_REF = reference_root()
 
 
 def available(ref: Path = DEFAULT_REF) -> bool:

@@ -443,6 +443,10 @@ int spe_create(int n, int device, spe_engine** out) {
   err = cudaMalloc(&e->tw, tw.size() * sizeof(float2));
   if (err == cudaSuccess) err = cudaMalloc(&e->A, e->npix * sizeof(float));
   if (err == cudaSuccess) err = cudaMemcpy(e->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  // a pageable host-to-device cudaMemcpy may return before the data has
+  // landed, and nothing orders it before kernels on the engine's
+  // non-blocking stream (which read the twiddles before griddepcontrol.wait)
+  if (err == cudaSuccess) err = cudaDeviceSynchronize();
   if (err != cudaSuccess) {
     cudaFree(e->tw);
     cudaFree(e->A);

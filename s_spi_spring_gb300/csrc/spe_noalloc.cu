@@ -11,8 +11,14 @@
 // point makes no cudaMalloc / cudaFree and calls no allocating library.
 //
 // The price: the scratch array (kScratchBytes, 16 MiB) and the twiddle
-// tables are reserved on every GPU that loads the library, until the process
-// exits; a call rejects populations whose scratch would not fit.
+// tables are reserved on every GPU that runs this entry point, until the
+// process exits; a call rejects populations whose scratch would not fit.
+// CUDA loads modules lazily (the default since CUDA 12.2): the first call on
+// a device loads this library's device code, and that is when the 16 MiB
+// array and the code are placed in device memory.  That first call can
+// therefore fail on a device that is already fully reserved, so callers make
+// it during start-up, before they reserve the device and before any stream
+// capture; later calls allocate nothing.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -46,7 +52,11 @@ float2 g_host_twiddles[kTwiddleCapacity];  // staging for the one-time upload
 // One-time set-up on the current device: the device addresses of the two
 // file-scope arrays (host code cannot use the symbols as addresses) and the
 // twiddle upload.  Runs on the first call per device, so that first call
-// must come before any stream capture.
+// must come before any stream capture.  The upload is a pageable
+// cudaMemcpy on the legacy stream, which may return before the data has
+// landed and is not ordered before kernels on a non-blocking caller stream
+// (whose kernels read the twiddles before griddepcontrol.wait), so the
+// set-up waits for the device before it marks the tables ready.
 int setup(int dev, DeviceState*& out) {
   std::lock_guard<std::mutex> lock(g_mutex);
   DeviceState& s = g_state[dev];
@@ -66,6 +76,7 @@ int setup(int dev, DeviceState*& out) {
       off += ops->tw_size;
     }
     CK(cudaMemcpy(s.twiddles, g_host_twiddles, off * sizeof(float2), cudaMemcpyHostToDevice), "twiddle upload");
+    CK(cudaDeviceSynchronize(), "twiddle upload");
     s.ready = true;
   }
   out = &s;
@@ -90,14 +101,22 @@ extern "C" int spe_iterate_noalloc(int n, void* density, const int32_t* support,
                 "(at most %zu individuals of this size per call)",
                 count, n, n, need, kScratchBytes, kScratchBytes / ((size_t)n * n * sizeof(float2)));
   if (count == 0) return SPE_OK;
+  int k = 0;
+  while (k < kNumSizes && kSizes[k] != n) ++k;
+  if (k == kNumSizes)
+    return fail(SPE_ERR_UNSUPPORTED, "pattern side %d has no twiddle table in the allocation-free entry point", n);
   int dev = 0;
   CK(cudaGetDevice(&dev), "cudaGetDevice");
   if (dev >= kMaxDevices) return fail(SPE_ERR_UNSUPPORTED, "device index %d above %d", dev, kMaxDevices - 1);
+  if (cuda_stream) {  // the kernels launch on the current device: the stream must belong to it
+    int sdev = -1;
+    CK(cudaStreamGetDevice(static_cast<cudaStream_t>(cuda_stream), &sdev), "cudaStreamGetDevice");
+    if (sdev != dev)
+      return fail(SPE_ERR_INVALID, "cuda_stream belongs to device %d, but the current device is %d", sdev, dev);
+  }
   DeviceState* s = nullptr;
   int rc = setup(dev, s);
   if (rc) return rc;
-  int k = 0;
-  while (kSizes[k] != n) ++k;
 
   spe::Ctx c{};
   c.n = n;

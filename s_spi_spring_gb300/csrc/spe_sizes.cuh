@@ -1,11 +1,53 @@
 // Size-specialised op sequences.  Each spe_size_<N>.cu instantiates this for
 // one pattern side so that the sizes compile in parallel.
 #pragma once
+#include <atomic>
+
 #include "spe_internal.h"
 #include "spe_kernels.cuh"
 #include "spe_pipe.cuh"
 
 namespace spe {
+
+// Per-device caches below are shared by every engine and host thread: they
+// are atomics, and what they cache (an attribute set, a count queried) is
+// the same whichever thread fills it first.
+inline int sm_count() {
+  static std::atomic<int> count[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 64) {
+    int c = 0;
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    return c > 0 ? c : 148;
+  }
+  int c = count[dev].load(std::memory_order_acquire);
+  if (c == 0) {
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    count[dev].store(c, std::memory_order_release);
+  }
+  return c;
+}
+
+// Shared-memory opt-in of one kernel, once per device.  `configured` must be
+// distinct per kernel instantiation: callers pass their own flag word.  Two
+// threads may both set the (idempotent) attributes; a thread that sees the
+// device's bit knows they are set.
+template <class K>
+cudaError_t configure(K kern, size_t smem, std::atomic<unsigned long long>& configured) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
+  if (!bit || !(configured.load(std::memory_order_acquire) & bit)) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    if (bit) configured.fetch_or(bit, std::memory_order_release);
+  }
+  return cudaSuccess;
+}
 
 template <int N, int AXIS, class Op>
 cudaError_t launch_pass(const Op& op, int count, cudaStream_t st, const float2* tw) {
@@ -17,45 +59,12 @@ cudaError_t launch_pass(const Op& op, int count, cudaStream_t st, const float2* 
   const size_t smem = C::SMEM;
   auto kern = pass_kernel<N, AXIS, Op>;
   // the dynamic shared-memory opt-in is per device and per kernel
-  static unsigned long long configured = 0ull;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  static std::atomic<unsigned long long> configured{0ull};
+  cudaError_t e = configure(kern, smem, configured);
   if (e != cudaSuccess) return e;
-  if (dev >= 64 || !((configured >> dev) & 1ull)) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
-    if (dev < 64) configured |= (1ull << dev);
-  }
   if (count <= 0) return cudaSuccess;
   kern<<<(unsigned)count * (N / W), NT, smem, st>>>(op, tw);
   return cudaGetLastError();
-}
-
-inline int sm_count() {
-  static int count[64] = {0};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 64 && count[dev] == 0) cudaDeviceGetAttribute(&count[dev], cudaDevAttrMultiProcessorCount, dev);
-  return dev < 64 ? count[dev] : 148;
-}
-
-// Shared-memory opt-in of one kernel, once per device.  `configured` must be
-// distinct per kernel instantiation: callers pass their own flag word.
-template <class K>
-cudaError_t configure(K kern, size_t smem, unsigned long long& configured) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev >= 64 || !((configured >> dev) & 1ull)) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
-    if (dev < 64) configured |= (1ull << dev);
-  }
-  return cudaSuccess;
 }
 
 // tile-width variants compiled per size: those whose tile fits in shared
@@ -125,17 +134,19 @@ struct DefaultTiles {  // what the autotuner picks for a population of ~32 M pix
 // persistent grid size: the CTAs that fit on all SMs at once (occupancy
 // queried once per kernel and device), never more than the tiles
 template <class K>
-int resident_ctas(K kern, int threads, size_t smem, int* cache) {
+int resident_ctas(K kern, int threads, size_t smem, std::atomic<int>* cache) {
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 64) dev = 63;
-  if (cache[dev] == 0) {
+  int r = cache[dev].load(std::memory_order_acquire);
+  if (r == 0) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess || per_sm < 1)
       per_sm = 1;
-    cache[dev] = per_sm * sm_count();
+    r = per_sm * sm_count();
+    cache[dev].store(r, std::memory_order_release);
   }
-  return cache[dev];
+  return r;
 }
 
 // launch with programmatic stream serialisation (the kernel's prologue
@@ -165,8 +176,8 @@ template <int N, int W, class Lay = LayCol<N, W>>
 cudaError_t launch_cols_project(const Ctx& c) {
   using P = ColCfg<N, W, Lay>;
   auto kern = k_cols_project<N, W, Lay>;
-  static unsigned long long configured = 0ull;
-  static int resident[64] = {0};
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
@@ -179,8 +190,8 @@ template <int N, int W, int UPD, class XLay = LayPad<N, W>>
 cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
   using P = RowCfg<N, W, XLay>;
   auto kern = k_rows_iterate<N, W, UPD, XLay>;
-  static unsigned long long configured = 0ull;
-  static int resident[64] = {0};
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
@@ -194,8 +205,8 @@ template <int N, int W>
 cudaError_t launch_cols_pair(const Ctx& c) {
   using P = PairCfg<N, W / 2>;
   auto kern = k_cols_pair<N, W / 2>;
-  static unsigned long long configured = 0ull;
-  static int resident[64] = {0};
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
@@ -208,8 +219,8 @@ template <int N, int W, int TPT>
 cudaError_t launch_cols_warp(const Ctx& c) {
   using P = WarpCfg<N, W, TPT>;
   auto kern = k_cols_warp<N, W, TPT>;
-  static unsigned long long configured = 0ull;
-  static int resident[64] = {0};
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);
@@ -222,8 +233,8 @@ template <int N, int W, int LOSS, bool GRAD>
 cudaError_t launch_cols_loss(const Ctx& c, float eps, double* partials) {
   using P = ColCfg<N, W>;
   auto kern = k_cols_loss<N, W, LOSS, GRAD>;
-  static unsigned long long configured = 0ull;
-  static int resident[64] = {0};
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
   cudaError_t e = configure(kern, P::SMEM, configured);
   if (e != cudaSuccess || c.count <= 0) return e;
   const int tiles = c.count * (N / W);

@@ -8,11 +8,15 @@ over whole generation ranges.
 import importlib.util
 import json
 import os
+import sys
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference/spring/alg_manager.py"
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.refroot import reference_root  # noqa: E402
+
+REF = str(reference_root() / "spring" / "alg_manager.py")
 
 CASES = [
     # alg, it, beta, it_ER, it_eval, it_stab, sigma, threshold, repetitions, decay_exp, start, end, generations
