@@ -374,6 +374,17 @@ int spe_get_schedule(spe_engine* e, int* chunk, int* lanes);
  * schedule. */
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows);
 
+/* Number of CUDA devices (0 when there is none: not an error).  Replaces
+ * GPU_utils::get_count / get_ids (src/gpu/gpu_utils.cu:13-30), which the
+ * front end reaches as spring_core.GPUtils (src/wrapper.cpp:459-484). */
+int spe_device_count(int* count);
+
+/* Name (GPU_utils::get_info, src/gpu/gpu_utils.cu:32-47) and PCI bus id
+ * ("DDDD:BB:DD.F") of a device; either output may be NULL.  The bus id maps
+ * the CUDA ordinal to the management library's handle for the utilisation
+ * query of GPU_utils::get_usage (src/gpu/gpu_utils.cu:52-94). */
+int spe_device_info(int device, char* name, int name_len, char* pci_bus_id, int bus_len);
+
 /* Allocation-free HIO / RAAR / ER (no counterpart in the reference).
  * For callers that may not allocate GPU memory while they run -- e.g. an
  * online analysis step inside a detector pipeline that reserves the whole

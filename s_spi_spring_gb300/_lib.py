@@ -43,6 +43,8 @@ class SpeMetrics(C.Structure):
 SIGNATURES = {
     "spe_last_error": (C.c_char_p, []),
     "spe_version": (_i, []),
+    "spe_device_count": (_i, [C.POINTER(_i)]),
+    "spe_device_info": (_i, [_i, C.c_char_p, _i, C.c_char_p, _i]),
     "spe_prepare_pattern": (_i, [_fp, _i, _i, _i, _i, _fp]),
     "spe_create": (_i, [_i, _i, C.POINTER(_vp)]),
     "spe_destroy": (_i, [_vp]),
@@ -194,6 +196,21 @@ def call(name, *args):
     if rc != SPE_OK:
         raise EngineError(name, rc, lib.spe_last_error().decode())
     return rc
+
+
+def device_count() -> int:
+    """CUDA devices visible to the process (0 without any)."""
+    n = _i(0)
+    call("spe_device_count", C.byref(n))
+    return int(n.value)
+
+
+def device_info(device: int) -> tuple[str, str]:
+    """(name, PCI bus id) of a CUDA device."""
+    name = C.create_string_buffer(256)
+    bus = C.create_string_buffer(64)
+    call("spe_device_info", int(device), name, 256, bus, 64)
+    return name.value.decode(), bus.value.decode()
 
 
 def fptr(a: np.ndarray):

@@ -409,6 +409,34 @@ const char* spe_last_error(void) { return g_err.c_str(); }
 
 int spe_version(void) { return 100; }
 
+int spe_device_count(int* count) {
+  if (!count) return fail(SPE_ERR_INVALID, "null argument");
+  *count = 0;
+  int n = 0;
+  const cudaError_t e = cudaGetDeviceCount(&n);
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) {
+    cudaGetLastError();  // no device is a valid answer, not an error
+    return SPE_OK;
+  }
+  CK(e, "cudaGetDeviceCount");
+  *count = n;
+  return SPE_OK;
+}
+
+int spe_device_info(int device, char* name, int name_len, char* pci_bus_id, int bus_len) {
+  int n = 0;
+  int rc = spe_device_count(&n);
+  if (rc) return rc;
+  if (device < 0 || device >= n) return fail(SPE_ERR_INVALID, "device %d not present (%d devices)", device, n);
+  if (name && name_len > 0) {
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    snprintf(name, (size_t)name_len, "%s", prop.name);
+  }
+  if (pci_bus_id && bus_len > 0) CK(cudaDeviceGetPCIBusId(pci_bus_id, bus_len, device), "cudaDeviceGetPCIBusId");
+  return SPE_OK;
+}
+
 int spe_prepare_pattern(const float* intensities, int n, int center_x, int center_y, int use_bounds,
                         float* amplitudes_out) {
   if (!intensities || !amplitudes_out || n <= 0) return fail(SPE_ERR_INVALID, "invalid pattern arguments");

@@ -122,6 +122,16 @@ class AlgorithmSchedule:
             seq += full + sw
         return seq + full + swa + full + swa_eval + self._seq(self.eval, gen_it)
 
+    def sequence_ipr(self, gen_it, update_support=True):
+        """The conventional-IPR op list: repetitions x [stab + main, SW], then
+        evaluation (``AlgManager.get_sequence_ipr``, ``alg_manager.py:147-168``)."""
+        full = self._seq(self.stab, gen_it) + self._seq(self.main, gen_it)
+        sw = [self.support.get(gen_it, self.start, self.end)] if update_support else []
+        seq = []
+        for _ in range(self.repetitions):
+            seq += full + sw
+        return seq + self._seq(self.eval, gen_it)
+
 
 # ---------------------------------------------------------------------------
 # the generation loop (spring/mpr.py)
@@ -301,3 +311,37 @@ class MemeticRun:
         while self.generation < target:
             self.step()
         return self
+
+
+class IPRRun(MemeticRun):
+    """``MPR.runIPR`` (``spring/mpr.py:452-557``): the conventional iterative
+    phase retrieval of every individual on its own -- per generation
+    shrink-wrap, alignment and average (for the statistics) and the IPR op
+    list; no crossover and no replacement."""
+
+    def start(self):
+        """``mpr.py:478-491``."""
+        sol = self.solver
+        sol.Evaluate(self.recs)
+        self.sort()
+        sol.set_sequence(self.algman.sequence_ipr(0, update_support=not self.s.refine))
+        self.recs = sol.Sequence(self.recs)
+        self.sort()
+        self.get_best()
+        self.get_average()
+        self._record(0.0)
+
+    def step(self):
+        """``mpr.py:495-524``."""
+        t0 = time.perf_counter()
+        sol, s = self.solver, self.s
+        self.generation += 1
+        if not s.refine:
+            self.recs = sol.SW(self.recs, *self.algman.support_params(self.generation))
+        self.sort()
+        self.get_best()
+        self.get_average()
+        sol.set_sequence(self.algman.sequence_ipr(self.generation, update_support=not s.refine))
+        self.recs = sol.Sequence(self.recs)
+        self.replcount = 0
+        self._record(time.perf_counter() - t0)

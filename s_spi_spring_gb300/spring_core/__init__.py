@@ -1,5 +1,6 @@
-"""Import path of the reference's compiled module: ``spring_core.phase_retrieval``
-and ``spring_core.pattern`` (reference ``src/wrapper.cpp:24-27, 318``)."""
-from . import pattern, phase_retrieval
+"""Import path of the reference's compiled module: ``spring_core.phase_retrieval``,
+``spring_core.pattern`` and ``spring_core.GPUtils`` (reference
+``src/wrapper.cpp:24-27, 318, 459-484``)."""
+from . import GPUtils, pattern, phase_retrieval
 
-__all__ = ["pattern", "phase_retrieval"]
+__all__ = ["GPUtils", "pattern", "phase_retrieval"]
