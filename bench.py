@@ -81,7 +81,10 @@ def parse():
                          "own) at 512^2 x 64, one warm-up iteration and one call of --plain-profile-iters")
     ap.add_argument("--plain-profile-iters", type=int, default=2)
     ap.add_argument("--pop-sweep", action="store_true", help="iteration rate against population size at 512^2")
-    ap.add_argument("--memetic-gens", type=int, default=2, help="generations of the memetic loop to time (0: skip)")
+    ap.add_argument("--memetic-gens", type=int, default=10,
+                    help="generations of the memetic loop to time (0: skip); 10 is the workload as specified")
+    ap.add_argument("--large-gens", type=int, default=1,
+                    help="generations of the 2048^2 x 128 memetic loop with refinement to time (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default tile widths and schedule")
     ap.add_argument("--tiles", default="", help="cols,rows tile widths (implies --no-tune)")
     ap.add_argument("--schedule", default="", help="chunk,lanes iteration schedule (implies --no-tune)")
@@ -510,6 +513,59 @@ def large_population(args, local):
             "rfactor_median": round(float(np.median([x["error_fourier"] for x in m])), 5)}
 
 
+def large_memetic(args, local):
+    """The large-population workload as specified, over a bounded number of
+    generations: 2048 x 2048, 128 individuals; per generation shrink-wrap,
+    alignment, average, crossover, the sequences on parents and children
+    (RAAR beta 0.87, 200 iterations per main step, ER, shrink-wrap sigma 3 ->
+    1.5 at threshold 0.1) and 20 fused Adam steps of gradient refinement on
+    parents and children before the replacement; the error sums in FP64.
+    Reports seconds per generation, the iterations run, the best R-factor,
+    and the reconstruction error of the best individual against the true
+    object after the reference's alignment (translation, global phase, twin;
+    relative L2 in float64 on the host)."""
+    import torch
+    from s_spi_spring_gb300 import synthetic
+    from s_spi_spring_gb300.memetic import MemeticRun, MemeticSettings
+    from s_spi_spring_gb300.spring_core.phase_retrieval import Solver
+    n, P = 2048, 128
+    I, obj, _ = synthetic.ellipsoid_cluster_pattern(seed=9, n=n, extent=480.0, photons=1e9, masked=0.25)
+    st = MemeticSettings(generations=20, popsize=P, alg="RAAR", it=200, beta=BETA, it_ER=40, it_eval=40, sigma=3.0,
+                         threshold=0.1, refine_steps=20)
+    sol = Solver(I, gpus=[local], seed=42)
+    recs = sol.InitializePop(P, 600, itemsize=[120.0, 540.0], nitems=[2, 8], exponent=[0.5, 0.5], scaling=[0.5, 1.5],
+                             phaserange=0)
+    sol.engine.reserve(3 * P + 4)
+    run = MemeticRun(sol, recs, st)
+    t0 = time.perf_counter()
+    run.start()
+    torch.cuda.synchronize()
+    t_start = time.perf_counter() - t0
+    iters = 0
+    t0 = time.perf_counter()
+    for _ in range(args.large_gens):
+        seq = run.algman.sequence(run.generation + 1, area=[1, 1])
+        iters += 2 * P * sum(int(p[0]) for name, p in seq if name in ("HIO", "RAAR", "ER"))
+        run.step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    best = run.recs[int(np.argmin([r.get_error() for r in run.recs]))]
+    slot = sol._resident(best)
+    sol.engine.reshift(slot, 1, -1, obj.astype(np.complex64), 0.0, 2.0)
+    best._device_changed()
+    d = best.get_density().astype(np.complex128)
+    err = float(np.linalg.norm(d - obj) / np.linalg.norm(obj))
+    return {"workload": "2048x2048 complex64, 128 individuals: RAAR beta 0.87 (200 iterations per main step) + "
+                        "ER + shrink-wrap + crossover + 20 fused Adam refinement steps per generation; "
+                        "ellipsoid-cluster object, 1e9 photons, 25% masked",
+            "generations_timed": args.large_gens, "s_first_sequence": round(t_start, 2),
+            "s_per_generation": round(dt / max(args.large_gens, 1), 2),
+            "iter_ind_per_s": round(iters / dt, 1) if dt > 0 else None,
+            "best_error": [round(h["best"], 6) for h in run.history],
+            "replaced": [h["replaced"] for h in run.history],
+            "reconstruction_error_vs_truth": round(err, 5)}
+
+
 def run_engine(args):
     import torch
     from s_spi_spring_gb300 import _lib
@@ -678,6 +734,11 @@ def run_engine(args):
             out["large_population"] = large_population(args, local)
         except Exception as ex:
             out["large_population"] = {"error": str(ex)[:300]}
+    if rank == 0 and args.large_gens > 0:
+        try:
+            out["large_memetic"] = large_memetic(args, local)
+        except Exception as ex:
+            out["large_memetic"] = {"error": str(ex)[:300]}
     if rank == 0 and args.refine:
         try:
             out["refinement"] = refinement(args, local)

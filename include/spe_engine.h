@@ -374,6 +374,16 @@ int spe_get_schedule(spe_engine* e, int* chunk, int* lanes);
  * schedule. */
 int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols, int* rows);
 
+/* Whether spe_create accepts pattern side n (SPE_OK) or rejects it
+ * (SPE_ERR_UNSUPPORTED); host only, no device needed.  compiled (may be
+ * NULL) receives 1 for the sides with a compiled register-resident plan
+ * (16, 32, 64, 128, 256, 384, 512, 768, 1024, 2048) and 0 for the sides the
+ * any-side kernels run (every other side whose prime factors are at most
+ * 257 and whose lines fit in shared memory, n <= 14079).  The reference
+ * accepts every side (cufftPlan2d, src/gpu/gpu_context.h:29); this query has
+ * no counterpart there. */
+int spe_side_supported(int n, int* compiled);
+
 /* Number of CUDA devices (0 when there is none: not an error).  Replaces
  * GPU_utils::get_count / get_ids (src/gpu/gpu_utils.cu:13-30), which the
  * front end reaches as spring_core.GPUtils (src/wrapper.cpp:459-484). */

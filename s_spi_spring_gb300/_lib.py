@@ -43,6 +43,7 @@ class SpeMetrics(C.Structure):
 SIGNATURES = {
     "spe_last_error": (C.c_char_p, []),
     "spe_version": (_i, []),
+    "spe_side_supported": (_i, [_i, C.POINTER(_i)]),
     "spe_device_count": (_i, [C.POINTER(_i)]),
     "spe_device_info": (_i, [_i, C.c_char_p, _i, C.c_char_p, _i]),
     "spe_prepare_pattern": (_i, [_fp, _i, _i, _i, _i, _fp]),
@@ -196,6 +197,16 @@ def call(name, *args):
     if rc != SPE_OK:
         raise EngineError(name, rc, lib.spe_last_error().decode())
     return rc
+
+
+def side_supported(n: int) -> str | None:
+    """"compiled" for a side with a compiled plan, "any" for one the any-side
+    kernels run, None when the engine rejects it."""
+    c = _i(0)
+    rc = load().spe_side_supported(int(n), C.byref(c))
+    if rc != SPE_OK:
+        return None
+    return "compiled" if c.value else "any"
 
 
 def device_count() -> int:

@@ -35,7 +35,7 @@ const SizeOps* size_ops(int n) {
     case 768: return size_ops_768();
     case 1024: return size_ops_1024();
     case 2048: return size_ops_2048();
-    default: return nullptr;
+    default: return size_ops_any(n);
   }
 }
 
@@ -409,6 +409,16 @@ const char* spe_last_error(void) { return g_err.c_str(); }
 
 int spe_version(void) { return 100; }
 
+int spe_side_supported(int n, int* compiled) {
+  if (compiled) *compiled = 0;
+  const spe::SizeOps* ops = n > 0 ? spe::size_ops(n) : nullptr;
+  if (!ops)
+    return fail(SPE_ERR_UNSUPPORTED, "pattern side %d is not supported: a side needs prime factors of at most 257 "
+                "and at most 14079 pixels", n);
+  if (compiled) *compiled = spe::size_ops_any(n) != ops;
+  return SPE_OK;
+}
+
 int spe_device_count(int* count) {
   if (!count) return fail(SPE_ERR_INVALID, "null argument");
   *count = 0;
@@ -450,7 +460,8 @@ int spe_create(int n, int device, spe_engine** out) {
   const spe::SizeOps* ops = spe::size_ops(n);
   if (!ops)
     return fail(SPE_ERR_UNSUPPORTED,
-                "pattern side %d has no compiled FFT plan (supported: 16,32,64,128,256,384,512,768,1024,2048)", n);
+                "pattern side %d is not supported: a side needs prime factors of at most 257 and at most 14079 "
+                "pixels (sides 16,32,64,128,256,384,512,768,1024,2048 run compiled plans)", n);
   int ndev = 0;
   CK(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
   if (device < 0 || device >= ndev) return fail(SPE_ERR_INVALID, "device %d not present (%d devices)", device, ndev);
@@ -467,7 +478,7 @@ int spe_create(int n, int device, spe_engine** out) {
   }
   e->st = e->own;
   std::vector<float2> tw(ops->tw_size);
-  ops->fill_tw(tw.data());
+  ops->fill_tw(tw.data(), n);
   err = cudaMalloc(&e->tw, tw.size() * sizeof(float2));
   if (err == cudaSuccess) err = cudaMalloc(&e->A, e->npix * sizeof(float));
   if (err == cudaSuccess) err = cudaMemcpy(e->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);

@@ -103,7 +103,9 @@ __device__ __forceinline__ float2 ctwiddle(float2 a) {
     constexpr float h = 0.70710678118654752440f;
     constexpr float c = ct_cos_frac(M, R) > 0 ? h : -h;
     constexpr float s = S * ct_sin_frac(M, R) > 0 ? h : -h;
-    return make_float2(c * a.x - s * a.y, c * a.y + s * a.x);
+    // written as explicit fused multiply-adds (not left to contraction) so
+    // that the paired-line kernels (spe_pairs.cuh) round identically
+    return make_float2(fmaf(c, a.x, -(s * a.y)), fmaf(c, a.y, s * a.x));
   } else {
     constexpr float c = float(ct_cos_frac(M, R));
     constexpr float s = float(S * ct_sin_frac(M, R));

@@ -74,7 +74,7 @@ struct SizeOps {
   int tiles_rows;  // CTAs per individual of a row pass
   int tiles_cols;  // CTAs per individual of a column pass
   int tw_size;     // twiddle table entries
-  void (*fill_tw)(float2*);
+  void (*fill_tw)(float2*, int n);  // tw_size entries for side n
   // upd: 0 HIO, 1 RAAR, 2 ER; wc / wr: tile widths of the column / row
   // pass of the iteration kernels (<= 0: defaults)
   cudaError_t (*iterate)(const Ctx&, int upd, int iterations, float beta, Gate g, int wc, int wr);
@@ -118,5 +118,9 @@ struct SizeOps {
 };
 
 const SizeOps* size_ops(int n);
+// sides without a compiled plan (spe_size_any.cu): the table of side n, or
+// null when n has a prime factor above the accepted bound or its lines do
+// not fit in shared memory
+const SizeOps* size_ops_any(int n);
 
 }  // namespace spe

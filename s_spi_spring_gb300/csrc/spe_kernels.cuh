@@ -62,7 +62,7 @@ __device__ __forceinline__ bool phase_out(float2 v, const GateK& g) {
 // hardware reciprocal square root (2 ulp; the reference is built with
 // --use_fast_math and divides approximately as well).
 __device__ __forceinline__ float2 project(float2 F, float a) {
-  const float m2 = F.y * F.y + F.x * F.x;
+  const float m2 = fmaf(F.x, F.x, F.y * F.y);  // explicit: the paired kernels round the same way
   if (a >= 0.f) {
     if (m2 > 0.f) {
       const float s = a * rsqrtf(m2);

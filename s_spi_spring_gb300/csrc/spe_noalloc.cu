@@ -72,7 +72,7 @@ int setup(int dev, DeviceState*& out) {
       if (!ops || off + ops->tw_size > kTwiddleCapacity)
         return spe_detail::fail(SPE_ERR_STATE, "twiddle tables exceed the static capacity");
       s.offset[k] = off;
-      ops->fill_tw(g_host_twiddles + off);
+      ops->fill_tw(g_host_twiddles + off, kSizes[k]);
       off += ops->tw_size;
     }
     CK(cudaMemcpy(s.twiddles, g_host_twiddles, off * sizeof(float2), cudaMemcpyHostToDevice), "twiddle upload");

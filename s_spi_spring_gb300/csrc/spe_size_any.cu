@@ -1,0 +1,610 @@
+// Pattern sides without a compiled plan: the same operations as the
+// size-specialised units (spe_sizes.cuh), with the side a run-time value.
+//
+// The reference plans any side with cuFFT (cufftPlan2d(n, n),
+// src/gpu/gpu_context.h:29), and its front end produces arbitrary sides:
+// the pattern is cropped to max(shape) by default and may be rescaled to any
+// size (spring/pattern_manager.py:61-84) -- the reference's own example
+// patterns of 1054 x 1024 become 1054 x 1054.  Sides with a compiled plan
+// (16 ... 2048, spe_sizes.cuh) keep their register-resident kernels; every
+// other side runs here.
+//
+// One pass kernel serves every operation: a CTA holds W whole lines (rows or
+// columns) of one individual in shared memory, applies the operation's load,
+// transforms, pointwise step and store (the same op functors as the
+// compiled passes), and reduces its partial sums.  The 1D transform is a
+// self-sorting Stockham FFT over the prime factors of the side (radix 4 where
+// the side has a factor 4): every pass computes each output as the direct
+// sum over its radix-R inputs with the combined twiddle
+//   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)),
+// k = b mod NS, from a table exp(2 pi i m / n) computed in double.  A pass
+// costs R complex multiply-adds per point, so a side with a large prime
+// factor p costs p per point: sides whose largest prime factor exceeds
+// kMaxPrime are rejected rather than run at that cost.
+#include <map>
+#include <memory>
+#include <mutex>
+
+#include "spe_sizes.cuh"
+
+namespace spe {
+namespace {
+
+constexpr int kAnyThreads = 512;
+constexpr int kMaxPrime = 257;       // largest prime factor accepted
+constexpr int kMaxRadices = 24;
+constexpr size_t kAnySmem = 220 * 1024;  // shared-memory budget of one CTA (two line buffers)
+
+struct AnyPlan {
+  int n;                  // side
+  int W;                  // lines per CTA
+  int LS;                 // shared-memory stride of a line (odd: conflict-free 8-byte columns)
+  int nrad;               // radix passes
+  int rad[kMaxRadices];   // radices in pass order
+};
+
+// out[c * LS + pos] for the W lines of the tile: one radix pass per factor,
+// ping-ponging between the two line buffers.  On return `cur` holds the
+// transform.
+template <int S>
+__device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPlan& pl,
+                                        const float2* __restrict__ tw, int nl) {
+  const int n = pl.n, LS = pl.LS;
+  int NS = 1;
+  for (int ps = 0; ps < pl.nrad; ++ps) {
+    const int R = pl.rad[ps];
+    const int m = n / R;        // butterflies; input stride
+    const int span = NS * R;    // outputs of one sub-transform
+    const int tstep = n / span; // twiddle-table step of one unit of (k + q NS)
+    for (int i = threadIdx.x; i < nl * n; i += kAnyThreads) {
+      const int c = i / n, pos = i - c * n;
+      const int j = pos / span, rem = pos - j * span;
+      const int q = rem / NS, k = rem - q * NS;
+      const float2* src = cur + c * LS + j * NS + k;
+      const int e = (k + q * NS) * tstep;  // < n
+      float2 acc = src[0];
+      int idx = 0;
+      for (int r = 1; r < R; ++r) {
+        idx += e;
+        if (idx >= n) idx -= n;
+        float2 w = __ldg(tw + idx);
+        if (S < 0) w.y = -w.y;
+        const float2 x = src[r * m];
+        acc.x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc.x));
+        acc.y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc.y));
+      }
+      oth[c * LS + pos] = acc;
+    }
+    __syncthreads();
+    float2* t = cur;
+    cur = oth;
+    oth = t;
+    NS *= R;
+  }
+}
+
+template <int AXIS, class Op>
+__global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPlan pl, const float2* __restrict__ tw) {
+  extern __shared__ float2 sm_any[];
+  const int n = pl.n, W = pl.W, LS = pl.LS;
+  float2* cur = sm_any;
+  float2* oth = sm_any + (size_t)W * LS;
+  const int tpi = (n + W - 1) / W;
+  const int p = op.first + blockIdx.x / tpi;
+  const int l0 = (blockIdx.x % tpi) * W;
+  const int nl = min(W, n - l0);
+  const size_t base = (size_t)p * n * n;
+  const int tot = nl * n;
+  typename Op::Acc acc;
+  // element i of the tile: row passes walk along x (whole rows), column
+  // passes across the tile's columns first (row segments of nl elements)
+  auto coords = [&](int i, int& c, int& l, int& y, int& x) {
+    if (AXIS == AX_ROWS) {
+      c = i / n;
+      l = i - c * n;
+      y = l0 + c;
+      x = l;
+    } else {
+      l = i / nl;
+      c = i - l * nl;
+      y = l;
+      x = l0 + c;
+    }
+  };
+  for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
+    int c, l, y, x;
+    coords(i, c, l, y, x);
+    cur[c * LS + l] = op.load(base + (size_t)y * n + x, p, y, x, acc);
+  }
+  __syncthreads();
+  if constexpr (Op::FFT1 != 0) fft_any<Op::FFT1>(cur, oth, pl, tw, nl);
+  if constexpr (Op::FFT2 != 0) {
+    for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
+      int c, l, y, x;
+      coords(i, c, l, y, x);
+      cur[c * LS + l] = op.mid(cur[c * LS + l], base + (size_t)y * n + x, p, y, x, acc);
+    }
+    __syncthreads();
+    fft_any<Op::FFT2>(cur, oth, pl, tw, nl);
+  }
+  for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
+    int c, l, y, x;
+    coords(i, c, l, y, x);
+    op.store(cur[c * LS + l], base + (size_t)y * n + x, p, y, x, acc);
+  }
+  if constexpr (Op::NSUM + Op::NMAX > 0) {
+    double r[NRED];
+    acc.values(r);
+    block_reduce_store<kAnyThreads, Op::NSUM, Op::NMAX>(op.partials, r);
+  }
+  if constexpr (Op::PEAK) block_argmax_store<kAnyThreads>(op.partials, acc.mx, acc.idx);
+}
+
+// ---------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------
+bool make_plan(int n, AnyPlan& pl) {
+  if (n < 2) return false;
+  pl.n = n;
+  pl.nrad = 0;
+  int m = n;
+  while (m % 4 == 0 && pl.nrad < kMaxRadices) {
+    pl.rad[pl.nrad++] = 4;
+    m /= 4;
+  }
+  for (int f = 2; f <= m && pl.nrad < kMaxRadices;) {
+    if (m % f == 0) {
+      if (f > kMaxPrime) return false;
+      pl.rad[pl.nrad++] = f;
+      m /= f;
+    } else {
+      f += (f == 2) ? 1 : 2;
+    }
+  }
+  if (m != 1) return false;
+  pl.LS = n | 1;
+  const size_t per_line = 2 * (size_t)pl.LS * sizeof(float2);
+  const size_t w = kAnySmem / per_line;
+  if (w < 1) return false;
+  pl.W = (int)(w < 8 ? w : 8);
+  return true;
+}
+
+struct AnyEntry {
+  AnyPlan plan;
+  SizeOps ops;
+};
+
+std::mutex g_any_mutex;
+std::map<int, std::unique_ptr<AnyEntry>> g_any;
+
+const AnyPlan& plan_of(int n) {
+  std::lock_guard<std::mutex> lock(g_any_mutex);
+  return g_any.at(n)->plan;
+}
+
+size_t smem_of(const AnyPlan& pl) { return 2 * (size_t)pl.W * pl.LS * sizeof(float2); }
+
+template <int AXIS, class Op>
+cudaError_t launch_any(const Op& op, const AnyPlan& pl, int count, cudaStream_t st, const float2* tw) {
+  auto kern = pass_any<AXIS, Op>;
+  static std::atomic<unsigned long long> configured{0ull};
+  const size_t smem = smem_of(pl);
+  // the attribute is set to the largest budget once: it is an upper bound
+  cudaError_t e = configure(kern, kAnySmem, configured);
+  if (e != cudaSuccess || count <= 0) return e;
+  const int tpi = (pl.n + pl.W - 1) / pl.W;
+  kern<<<(unsigned)count * tpi, kAnyThreads, smem, st>>>(op, pl, tw);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// the operation table (the sequences of SizeImpl, spe_sizes.cuh, on pass_any)
+// ---------------------------------------------------------------------------
+struct SizeAny {
+  static float scale(int n) { return (float)(1.0 / ((double)n * (double)n)); }
+
+  template <int SRC>
+  static OpRowsForward<SRC> rows_forward(const Ctx& c, const float2* src, float2* dst, Gate g, double* partials) {
+    OpRowsForward<SRC> op;
+    op.first = c.first;
+    op.partials = partials;
+    op.rho = src;
+    op.S = c.S;
+    op.T = dst;
+    op.g = g;
+    return op;
+  }
+
+  static OpColsProject cols_project(const Ctx& c) {
+    OpColsProject op;
+    op.first = c.first;
+    op.partials = nullptr;
+    op.T = c.T;
+    op.A = c.A;
+    op.n = c.n;
+    op.ipp = c.ipp;
+    return op;
+  }
+
+  template <int UPD>
+  static cudaError_t iterate_t(const Ctx& c, int iters, float beta, Gate g) {
+    const AnyPlan& pl = plan_of(c.n);
+    SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_RHO>(c, c.rho, c.T, g, nullptr), pl, c.count, c.st, c.tw)));
+    const OpColsProject proj = cols_project(c);
+    OpRowsIterate<UPD> it;
+    it.first = c.first;
+    it.partials = nullptr;
+    it.T = c.T;
+    it.rho = c.rho;
+    it.S = c.S;
+    it.scale = scale(c.n);
+    it.beta = beta;
+    it.g = g;
+    for (int i = 0; i < iters; ++i) {
+      SPE_TRY((launch_any<AX_COLS>(proj, pl, c.count, c.st, c.tw)));
+      if (i == 0 && c.mark) SPE_TRY(cudaEventRecord(c.mark, c.st));
+      SPE_TRY((launch_any<AX_ROWS>(it, pl, c.count, c.st, c.tw)));
+    }
+    SPE_TRY((launch_any<AX_COLS>(proj, pl, c.count, c.st, c.tw)));
+    if (iters == 0 && c.mark) SPE_TRY(cudaEventRecord(c.mark, c.st));
+    OpRowsFinal fin;
+    fin.first = c.first;
+    fin.partials = nullptr;
+    fin.T = c.T;
+    fin.out = c.rho;
+    fin.scale = scale(c.n);
+    return launch_any<AX_ROWS>(fin, pl, c.count, c.st, c.tw);
+  }
+
+  // tile widths are fixed by the plan: wc / wr are ignored
+  static cudaError_t iterate(const Ctx& c, int upd, int iters, float beta, Gate g, int, int) {
+    switch (upd) {
+      case 0: return iterate_t<UPD_HIO>(c, iters, beta, g);
+      case 1: return iterate_t<UPD_RAAR>(c, iters, beta, g);
+      default: return iterate_t<UPD_ER>(c, iters, beta, g);
+    }
+  }
+
+  static int one_width(int* out) {
+    out[0] = 0;
+    return 1;
+  }
+
+  static cudaError_t blur_magnitude(const Ctx& c, float sigma_ft) {
+    const AnyPlan& pl = plan_of(c.n);
+    const Gate g{};
+    SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_RHO>(c, c.rho, c.T, g, nullptr), pl, c.count, c.st, c.tw)));
+    SPE_TRY((launch_any<AX_COLS>(cols_project(c), pl, c.count, c.st, c.tw)));
+    OpRowsModulusForward mf;
+    mf.first = c.first;
+    mf.partials = nullptr;
+    mf.T = c.T;
+    mf.scale = scale(c.n);
+    SPE_TRY((launch_any<AX_ROWS>(mf, pl, c.count, c.st, c.tw)));
+    OpColsBlur bl;
+    bl.first = c.first;
+    bl.partials = nullptr;
+    bl.T = c.T;
+    bl.n = c.n;
+    bl.sig2 = sigma_ft * sigma_ft;
+    SPE_TRY((launch_any<AX_COLS>(bl, pl, c.count, c.st, c.tw)));
+    OpRowsMagnitude mg;
+    mg.first = c.first;
+    mg.partials = c.partials;
+    mg.T = c.T;
+    mg.M = c.M;
+    return launch_any<AX_ROWS>(mg, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t error_terms(const Ctx& c, Gate g, double* p1, double* p2, double* p3) {
+    const AnyPlan& pl = plan_of(c.n);
+    SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_GATED>(c, c.rho, c.T, g, p1), pl, c.count, c.st, c.tw)));
+    OpColsError ce;
+    ce.first = c.first;
+    ce.partials = p2;
+    ce.T = c.T;
+    ce.A = c.A;
+    ce.n = c.n;
+    ce.ipp = c.ipp;
+    SPE_TRY((launch_any<AX_COLS>(ce, pl, c.count, c.st, c.tw)));
+    OpRowsRealError re;
+    re.first = c.first;
+    re.partials = p3;
+    re.T = c.T;
+    re.S = c.S;
+    re.scale = scale(c.n);
+    re.g = g;
+    return launch_any<AX_ROWS>(re, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t abs_spectrum(const Ctx& c, float2* dst) {
+    const AnyPlan& pl = plan_of(c.n);
+    const Gate g{};
+    SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_ABS>(c, c.rho, dst, g, nullptr), pl, c.count, c.st, c.tw)));
+    OpColsForward cf;
+    cf.first = c.first;
+    cf.partials = nullptr;
+    cf.src = dst;
+    cf.dst = dst;
+    return launch_any<AX_COLS>(cf, pl, c.count, c.st, c.tw);
+  }
+
+  template <int SIGN>
+  static cudaError_t corr_peak_t(const Ctx& c, const float2* D, const float2* Dref, size_t ref_stride, int ref_first,
+                                 float minr, float maxr, int norm_d, int norm_ref, double* partials) {
+    const AnyPlan& pl = plan_of(c.n);
+    OpColsCrossPower<SIGN> cp;
+    cp.first = c.first;
+    cp.partials = nullptr;
+    cp.D = D;
+    cp.Dref = Dref;
+    cp.ref_stride = ref_stride;
+    cp.ref_first = ref_first;
+    cp.dst = c.T;
+    cp.A = c.A;
+    cp.n = c.n;
+    cp.ipp = c.ipp;
+    cp.minr = minr;
+    cp.maxr = maxr;
+    cp.norm_d = norm_d;
+    cp.norm_ref = norm_ref;
+    SPE_TRY((launch_any<AX_COLS>(cp, pl, c.count, c.st, c.tw)));
+    OpRowsPeak pk;
+    pk.first = c.first;
+    pk.partials = partials;
+    pk.T = c.T;
+    pk.n = c.n;
+    return launch_any<AX_ROWS>(pk, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t corr_peak(const Ctx& c, const float2* D, const float2* Dref, size_t ref_stride, int ref_first,
+                               int sign, float minr, float maxr, int norm_d, int norm_ref, double* partials) {
+    if (sign < 0) return corr_peak_t<-1>(c, D, Dref, ref_stride, ref_first, minr, maxr, norm_d, norm_ref, partials);
+    return corr_peak_t<+1>(c, D, Dref, ref_stride, ref_first, minr, maxr, norm_d, norm_ref, partials);
+  }
+
+  // ---- generic transforms over `c.count` items starting at `data` (c.first ignored)
+  static cudaError_t fft2(const Ctx& c, float2* data, int sign) {
+    const AnyPlan& pl = plan_of(c.n);
+    if (sign > 0) {
+      Ctx z = c;
+      z.first = 0;
+      SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_RHO>(z, data, data, Gate{}, nullptr), pl, c.count, c.st, c.tw)));
+      OpColsTransform<+1> ct;
+      ct.first = 0;
+      ct.partials = nullptr;
+      ct.src = data;
+      ct.dst = data;
+      return launch_any<AX_COLS>(ct, pl, c.count, c.st, c.tw);
+    }
+    OpColsTransform<-1> ct;
+    ct.first = 0;
+    ct.partials = nullptr;
+    ct.src = data;
+    ct.dst = data;
+    SPE_TRY((launch_any<AX_COLS>(ct, pl, c.count, c.st, c.tw)));
+    OpRowsFinal fin;
+    fin.first = 0;
+    fin.partials = nullptr;
+    fin.T = data;
+    fin.out = data;
+    fin.scale = scale(c.n);
+    return launch_any<AX_ROWS>(fin, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t ft_magnitude(const Ctx& c, const float2* src, float2* tmp, float* M) {
+    const AnyPlan& pl = plan_of(c.n);
+    Ctx z = c;
+    z.first = 0;
+    SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_RHO>(z, src, tmp, Gate{}, nullptr), pl, c.count, c.st, c.tw)));
+    OpColsMagnitude cm;
+    cm.first = 0;
+    cm.partials = nullptr;
+    cm.src = tmp;
+    cm.M = M;
+    return launch_any<AX_COLS>(cm, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t abs_spectrum_items(const Ctx& c, const float2* src, float2* dst) {
+    const AnyPlan& pl = plan_of(c.n);
+    Ctx z = c;
+    z.first = 0;
+    SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_ABS>(z, src, dst, Gate{}, nullptr), pl, c.count, c.st, c.tw)));
+    OpColsTransform<+1> ct;
+    ct.first = 0;
+    ct.partials = nullptr;
+    ct.src = dst;
+    ct.dst = dst;
+    return launch_any<AX_COLS>(ct, pl, c.count, c.st, c.tw);
+  }
+
+  template <int SIGN>
+  static cudaError_t corr_peak_idx_t(const Ctx& c, const float2* D, const float2* Dref, const int* xi, const int* ri,
+                                     float minr, float maxr, int norm_d, int norm_ref, float2* scratch,
+                                     double* partials) {
+    const AnyPlan& pl = plan_of(c.n);
+    OpColsCrossPowerIdx<SIGN> cp;
+    cp.first = 0;
+    cp.partials = nullptr;
+    cp.D = D;
+    cp.Dref = Dref;
+    cp.xi = xi;
+    cp.ri = ri;
+    cp.dst = scratch;
+    cp.A = c.A;
+    cp.n = c.n;
+    cp.minr = minr;
+    cp.maxr = maxr;
+    cp.norm_d = norm_d;
+    cp.norm_ref = norm_ref;
+    SPE_TRY((launch_any<AX_COLS>(cp, pl, c.count, c.st, c.tw)));
+    OpRowsPeak pk;
+    pk.first = 0;
+    pk.partials = partials;
+    pk.T = scratch;
+    pk.n = c.n;
+    return launch_any<AX_ROWS>(pk, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t corr_peak_idx(const Ctx& c, const float2* D, const float2* Dref, const int* xi, const int* ri,
+                                   int sign, float minr, float maxr, int norm_d, int norm_ref, float2* scratch,
+                                   double* partials) {
+    if (sign < 0) return corr_peak_idx_t<-1>(c, D, Dref, xi, ri, minr, maxr, norm_d, norm_ref, scratch, partials);
+    return corr_peak_idx_t<+1>(c, D, Dref, xi, ri, minr, maxr, norm_d, norm_ref, scratch, partials);
+  }
+
+  static cudaError_t known_power(const Ctx& c, double* partials) {
+    const AnyPlan& pl = plan_of(c.n);
+    SPE_TRY((launch_any<AX_ROWS>(rows_forward<SRC_RHO>(c, c.rho, c.T, Gate{}, nullptr), pl, c.count, c.st, c.tw)));
+    OpColsKnownPower kp;
+    kp.first = c.first;
+    kp.partials = partials;
+    kp.T = c.T;
+    kp.A = c.A;
+    kp.n = c.n;
+    kp.ipp = c.ipp;
+    return launch_any<AX_COLS>(kp, pl, c.count, c.st, c.tw);
+  }
+
+  // far-field loss: one partial per column tile (loss_tiles = tiles_cols)
+  template <int LOSS>
+  static cudaError_t loss_grad_t(const Ctx& c, float eps, double* partials, float2* grad, const float* scale) {
+    const AnyPlan& pl = plan_of(c.n);
+    OpRowsSupportForward rf;
+    rf.first = c.first;
+    rf.partials = nullptr;
+    rf.rho = c.rho;
+    rf.S = c.S;
+    rf.T = c.T;
+    SPE_TRY((launch_any<AX_ROWS>(rf, pl, c.count, c.st, c.tw)));
+    if (!grad) {
+      OpColsLoss<LOSS, false> cl;
+      cl.first = c.first;
+      cl.partials = partials;
+      cl.T = c.T;
+      cl.A = c.A;
+      cl.n = c.n;
+      cl.ipp = c.ipp;
+      cl.eps = eps;
+      return launch_any<AX_COLS>(cl, pl, c.count, c.st, c.tw);
+    }
+    OpColsLoss<LOSS, true> cl;
+    cl.first = c.first;
+    cl.partials = partials;
+    cl.T = c.T;
+    cl.A = c.A;
+    cl.n = c.n;
+    cl.ipp = c.ipp;
+    cl.eps = eps;
+    SPE_TRY((launch_any<AX_COLS>(cl, pl, c.count, c.st, c.tw)));
+    OpRowsGradOut go;
+    go.first = c.first;
+    go.partials = nullptr;
+    go.T = c.T;
+    go.S = c.S;
+    go.G = grad;
+    go.scale = scale;
+    return launch_any<AX_ROWS>(go, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t loss_grad(const Ctx& c, int loss, float eps, double* partials, float2* grad,
+                               const float* scale) {
+    return loss == LOSS_POISSON ? loss_grad_t<LOSS_POISSON>(c, eps, partials, grad, scale)
+                                : loss_grad_t<LOSS_AMPLITUDE>(c, eps, partials, grad, scale);
+  }
+
+  template <int LOSS>
+  static cudaError_t adam_step_t(const Ctx& c, float eps, double* partials, float2* m, float2* v, float b1, float b2,
+                                 float step_size, float inv_sqrt_bc2, float adam_eps) {
+    const AnyPlan& pl = plan_of(c.n);
+    OpRowsSupportForward rf;
+    rf.first = c.first;
+    rf.partials = nullptr;
+    rf.rho = c.rho;
+    rf.S = c.S;
+    rf.T = c.T;
+    SPE_TRY((launch_any<AX_ROWS>(rf, pl, c.count, c.st, c.tw)));
+    OpColsLoss<LOSS, true> cl;
+    cl.first = c.first;
+    cl.partials = partials;
+    cl.T = c.T;
+    cl.A = c.A;
+    cl.n = c.n;
+    cl.ipp = c.ipp;
+    cl.eps = eps;
+    SPE_TRY((launch_any<AX_COLS>(cl, pl, c.count, c.st, c.tw)));
+    OpRowsGradAdam ad;
+    ad.first = c.first;
+    ad.partials = nullptr;
+    ad.T = c.T;
+    ad.S = c.S;
+    ad.rho = c.rho;
+    ad.m = m;
+    ad.v = v;
+    ad.b1 = b1;
+    ad.b2 = b2;
+    ad.step_size = step_size;
+    ad.inv_sqrt_bc2 = inv_sqrt_bc2;
+    ad.eps = adam_eps;
+    return launch_any<AX_ROWS>(ad, pl, c.count, c.st, c.tw);
+  }
+
+  static cudaError_t adam_step(const Ctx& c, int loss, float eps, double* partials, float2* m, float2* v, float b1,
+                               float b2, float step_size, float inv_sqrt_bc2, float adam_eps) {
+    return loss == LOSS_POISSON
+               ? adam_step_t<LOSS_POISSON>(c, eps, partials, m, v, b1, b2, step_size, inv_sqrt_bc2, adam_eps)
+               : adam_step_t<LOSS_AMPLITUDE>(c, eps, partials, m, v, b1, b2, step_size, inv_sqrt_bc2, adam_eps);
+  }
+};
+
+// exp(+2 pi i m / n), m < n, double angles rounded once to float
+void fill_any(float2* out, int n) {
+  for (int m = 0; m < n; ++m) {
+    const double a = 2.0 * kPi * (double)m / (double)n;
+    out[m] = make_float2((float)cos(a), (float)sin(a));
+  }
+}
+
+}  // namespace
+
+bool any_side_supported(int n) {
+  AnyPlan pl;
+  return make_plan(n, pl);
+}
+
+const SizeOps* size_ops_any(int n) {
+  std::lock_guard<std::mutex> lock(g_any_mutex);
+  auto it = g_any.find(n);
+  if (it != g_any.end()) return &it->second->ops;
+  std::unique_ptr<AnyEntry> en(new AnyEntry());
+  if (!make_plan(n, en->plan)) return nullptr;
+  const int tiles = (n + en->plan.W - 1) / en->plan.W;
+  en->ops = SizeOps{n,
+                    tiles,
+                    tiles,
+                    n,
+                    &fill_any,
+                    &SizeAny::iterate,
+                    &SizeAny::blur_magnitude,
+                    &SizeAny::error_terms,
+                    &SizeAny::abs_spectrum,
+                    &SizeAny::corr_peak,
+                    &SizeAny::fft2,
+                    &SizeAny::ft_magnitude,
+                    &SizeAny::abs_spectrum_items,
+                    &SizeAny::corr_peak_idx,
+                    &SizeAny::one_width,
+                    &SizeAny::one_width,
+                    0,
+                    0,
+                    &SizeAny::known_power,
+                    &SizeAny::loss_grad,
+                    tiles,
+                    &SizeAny::adam_step};
+  const SizeOps* out = &en->ops;
+  g_any.emplace(n, std::move(en));
+  return out;
+}
+
+}  // namespace spe

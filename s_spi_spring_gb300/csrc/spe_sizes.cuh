@@ -6,6 +6,7 @@
 #include "spe_internal.h"
 #include "spe_kernels.cuh"
 #include "spe_pipe.cuh"
+#include "spe_pairs.cuh"
 
 namespace spe {
 
@@ -121,6 +122,22 @@ template <int N, int W>
 constexpr bool groupcol_ok() {
   return Plan<N>::TPT > 32 && cm_ok<N, W, Plan<N>::TPT>();
 }
+// paired-line variants (spe_pairs.cuh): sides 256, 512, 1024 (first radix 8,
+// at most 8 elements per thread); WP column pairs / WR row pairs per tile
+template <int N>
+constexpr bool pairs_side_ok() {
+  return N == 256 || N == 512 || N == 1024;
+}
+template <int N, int WP, bool PF>
+constexpr bool paircol_ok() {
+  return pairs_side_ok<N>() && WP >= 4 && N % (2 * WP) == 0 && PairColCfg<N, WP, PF>::NT <= 1024 &&
+         PairColCfg<N, WP, PF>::SMEM <= kMaxSmem;
+}
+template <int N, int WR>
+constexpr bool pairrow_ok() {
+  return pairs_side_ok<N>() && N % (2 * WR) == 0 && PairRowCfg<N, WR>::NT % 32 == 0 &&
+         PairRowCfg<N, WR>::NT <= 1024 && PairRowCfg<N, WR>::SMEM <= kMaxSmem;
+}
 constexpr int kColWidths[3] = {4, 8, 16};
 constexpr int kRowWidths[5] = {1, 2, 4, 8, 16};
 
@@ -201,6 +218,35 @@ cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
                     scale, beta, g, c.tw);
 }
 
+template <int N, int WP, bool PF>
+cudaError_t launch_cols_pairs(const Ctx& c) {
+  using P = PairColCfg<N, WP, PF>;
+  auto kern = k_cols_pairs<N, WP, PF>;
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / P::W);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
+  const int grid = tiles < slots ? tiles : slots;
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, c.tw);
+}
+
+template <int N, int WR, int UPD>
+cudaError_t launch_rows_pairs(const Ctx& c, float scale, float beta, Gate g) {
+  using P = PairRowCfg<N, WR>;
+  auto kern = k_rows_pairs<N, WR, UPD>;
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / P::ROWS);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
+  const int grid = tiles < slots ? tiles : slots;
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.rho, static_cast<const int*>(c.S), c.first, c.count,
+                    scale, beta, g, c.tw);
+}
+
 template <int N, int W>
 cudaError_t launch_cols_pair(const Ctx& c) {
   using P = PairCfg<N, W / 2>;
@@ -247,10 +293,16 @@ cudaError_t launch_cols_loss(const Ctx& c, float eps, double* partials) {
 // W < 0 two columns per thread, -W columns per tile; 100 + W one warp per
 // column, 200 + W the plan's threads per column (column-major tile, barrier
 // per column), 300 + W one column per thread with the padded layout, W
-// columns per tile
+// columns per tile; 400 + W column pairs with split real / imaginary parts
+// (spe_pairs.cuh), 500 + W the same with the next tile prefetched into
+// registers
 template <int N>
 cudaError_t launch_cols_w(const Ctx& c, int w) {
   switch (w) {
+    case 408: if constexpr (paircol_ok<N, 4, false>()) return launch_cols_pairs<N, 4, false>(c); break;
+    case 416: if constexpr (paircol_ok<N, 8, false>()) return launch_cols_pairs<N, 8, false>(c); break;
+    case 508: if constexpr (paircol_ok<N, 4, true>()) return launch_cols_pairs<N, 4, true>(c); break;
+    case 516: if constexpr (paircol_ok<N, 8, true>()) return launch_cols_pairs<N, 8, true>(c); break;
     case 104: if constexpr (warpcol_ok<N, 4>()) return launch_cols_warp<N, 4, 32>(c); break;
     case 108: if constexpr (warpcol_ok<N, 8>()) return launch_cols_warp<N, 8, 32>(c); break;
     case 116: if constexpr (warpcol_ok<N, 16>()) return launch_cols_warp<N, 16, 32>(c); break;
@@ -269,9 +321,15 @@ cudaError_t launch_cols_w(const Ctx& c, int w) {
   return cudaErrorInvalidValue;
 }
 
+// row-pass variant code: W rows per tile, one row per W threads groups;
+// 100 + W the per-exchange padding; 400 + W row pairs with split real /
+// imaginary parts (spe_pairs.cuh)
 template <int N, int UPD>
 cudaError_t launch_rows_w(const Ctx& c, int w, float scale, float beta, Gate g) {
   switch (w) {
+    case 402: if constexpr (pairrow_ok<N, 1>()) return launch_rows_pairs<N, 1, UPD>(c, scale, beta, g); break;
+    case 404: if constexpr (pairrow_ok<N, 2>()) return launch_rows_pairs<N, 2, UPD>(c, scale, beta, g); break;
+    case 408: if constexpr (pairrow_ok<N, 4>()) return launch_rows_pairs<N, 4, UPD>(c, scale, beta, g); break;
     case 1: if constexpr (row_ok<N, 1>()) return launch_rows_iterate<N, 1, UPD>(c, scale, beta, g); break;
     case 2: if constexpr (row_ok<N, 2>()) return launch_rows_iterate<N, 2, UPD>(c, scale, beta, g); break;
     case 4: if constexpr (row_ok<N, 4>()) return launch_rows_iterate<N, 4, UPD>(c, scale, beta, g); break;
@@ -291,6 +349,11 @@ cudaError_t launch_rows_w(const Ctx& c, int w, float scale, float beta, Gate g) 
     cudaError_t e_ = (x);                  \
     if (e_ != cudaSuccess) return e_;      \
   } while (0)
+
+template <int N>
+void fill_twiddles_n(float2* out, int) {
+  fill_twiddles<N>(out);
+}
 
 template <int N>
 struct SizeImpl {
@@ -361,6 +424,10 @@ struct SizeImpl {
 
   static int col_widths(int* out) {
     int k = 0;
+    if constexpr (paircol_ok<N, 4, false>()) out[k++] = 408;
+    if constexpr (paircol_ok<N, 8, false>()) out[k++] = 416;
+    if constexpr (paircol_ok<N, 4, true>()) out[k++] = 508;
+    if constexpr (paircol_ok<N, 8, true>()) out[k++] = 516;
     if constexpr (warpcol_ok<N, 4>()) out[k++] = 104;
     if constexpr (warpcol_ok<N, 8>()) out[k++] = 108;
     if constexpr (warpcol_ok<N, 16>()) out[k++] = 116;
@@ -378,6 +445,9 @@ struct SizeImpl {
   }
   static int row_widths(int* out) {
     int k = 0;
+    if constexpr (pairrow_ok<N, 1>()) out[k++] = 402;
+    if constexpr (pairrow_ok<N, 2>()) out[k++] = 404;
+    if constexpr (pairrow_ok<N, 4>()) out[k++] = 408;
     if constexpr (row_ok<N, 1>()) out[k++] = 1;
     if constexpr (row_ok<N, 2>()) out[k++] = 2;
     if constexpr (row_ok<N, 4>()) out[k++] = 4;
@@ -652,7 +722,7 @@ struct SizeImpl {
                               N / TileW<N>::rows,
                               N / TileW<N>::cols,
                               TwiddleTable<N>::size(),
-                              &fill_twiddles<N>,
+                              &fill_twiddles_n<N>,
                               &SizeImpl<N>::iterate,
                               &SizeImpl<N>::blur_magnitude,
                               &SizeImpl<N>::error_terms,

@@ -166,6 +166,13 @@ class MemeticSettings:
     crossexp: float = 1.0
     crossft: float = 1.0
     refine: bool = False
+    # gradient refinement interleaved with the generations (no reference
+    # counterpart): after each generation's sequences, `refine_steps` fused
+    # Adam steps on the far-field loss of parents and children, before the
+    # replacement compares their errors
+    refine_steps: int = 0
+    refine_lr: float = 1e-3
+    refine_loss: str = "poisson"
 
     def schedule(self) -> AlgorithmSchedule:
         """``MPR.InitIA`` (``mpr.py:110-140``)."""
@@ -287,6 +294,9 @@ class MemeticRun:
         sol.set_sequence(self.algman.sequence(self.generation, area=suppix, update_support=not s.refine))
         self.recs = sol.Sequence(self.recs)
         new = sol.Sequence(new)
+        if s.refine_steps > 0:
+            self.recs = sol.Refine(self.recs, s.refine_steps, s.refine_lr, s.refine_loss)
+            new = sol.Refine(new, s.refine_steps, s.refine_lr, s.refine_loss)
         repl = np.zeros(len(self.recs))
         for i in range(len(new)):
             iold = i % len(self.recs)

@@ -411,6 +411,26 @@ class Solver:
             r._set_metrics(m)
         return None
 
+    # -- gradient refinement (no reference counterpart) -------------------------
+    def Refine(self, reconstruction, steps=50, lr=1e-3, loss="poisson", eps=1e-6):
+        """`steps` fused Adam steps on the far-field loss of each
+        reconstruction (``s_spi_spring_gb300.refine.refine``, on the
+        individuals' device slots), then the metrics of ``Evaluate`` so that
+        the errors the generation loop compares are those of the refined
+        densities."""
+        from .refine import refine
+        import torch
+        recs, single = _as_list(reconstruction)
+        if recs and steps > 0:
+            first = self._stage(recs)
+            refine(self.engine, first, len(recs), steps=int(steps), lr=lr, loss=loss, eps=eps,
+                   device=torch.device("cuda", self.device))
+            for r in recs:
+                r._device_changed()
+            self._settle()
+            self.Evaluate(recs)
+        return recs[0] if single else recs
+
     # -- starting populations (src/solver.cpp:824-957, wrapper.cpp:278-298) ------
     def InitializePop(self, popsize, suppsize, itemsize, nitems=8, exponent=0, scaling=0, phaserange=0, suppcut=0):
         """``Solver::Initialize_pop``: `popsize` random starting individuals."""

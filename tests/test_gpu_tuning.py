@@ -1,10 +1,11 @@
 """Tile-width variants of the iteration kernels and the autotuner.
 
 Every compiled tile width -- including the column pass that keeps two
-columns per thread (negative widths) and the one with a warp per column
-(100 + width) -- performs the same per-element
-arithmetic, so all variants must give bit-identical results; the autotuner
-must leave the population as it found it."""
+columns per thread (negative widths), the one with a warp per column
+(100 + width) and the paired-line passes with split real and imaginary parts
+(400 + width, and 500 + width with register prefetch) -- performs the same
+per-element arithmetic, so all variants must give bit-identical results; the
+autotuner must leave the population as it found it."""
 import itertools
 
 import numpy as np
@@ -31,8 +32,8 @@ def test_all_tile_widths_bit_identical(n):
     e, dens, S = engine(n, P)
     ref = None
     tried = 0
-    for wc, wr in itertools.product([4, 8, 16, -4, -8, -16, 104, 108, 116, 204, 208, 304, 308],
-                                    [1, 2, 4, 8, 16, 101, 102, 104, 108]):
+    for wc, wr in itertools.product([4, 8, 16, -4, -8, -16, 104, 108, 116, 204, 208, 304, 308, 408, 416, 508, 516],
+                                    [1, 2, 4, 8, 16, 101, 102, 104, 108, 402, 404, 408]):
         try:
             e.set_tiles(wc, wr)
         except _lib.EngineError:

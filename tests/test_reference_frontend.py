@@ -216,3 +216,33 @@ def test_gputils_interface_without_devices():
     if n:
         pytest.skip("a GPU is visible")
     assert GPUtils.get_ids() == [] and GPUtils.get_info() == [] and GPUtils.get_usage() == []
+
+
+def test_reference_example_patterns_have_supported_sides(reference_frontend):
+    """The reference's bundled example patterns, prepared by its own Pattern
+    class with the default crop (max of the shape) and with the crops its
+    Pattern notebook uses, give sides the engine accepts
+    (examples/Pattern.ipynb:75, 231-233; rescaling with size= runs the
+    mirror's resampling on the GPU, tests/test_gpu_pattern.py)."""
+    import glob
+    mpr, pm, sm = reference_frontend
+    files = sorted(glob.glob(str(REF / "examples" / "data" / "*.npz")))
+    if not files:
+        pytest.skip("the reference's example data are absent")
+    try:
+        _lib.load()
+    except ImportError:
+        pytest.skip("engine library not built")
+    sides = set()
+    for f in (files[0], files[-1]):  # one of each geometry (A: 1024 x 1024, B: 1054 x 1024)
+        d = np.load(f)
+        for kw in ({}, {"cropsize": 1200}, {"cropsize": 600}):
+            p = pm.Pattern(pattern=d["pattern"], mask=d["mask"], center=d["center"], pid=d["pid"], satvalue=3e4,
+                           **kw)
+            n = p.get().shape[0]
+            assert p.get().shape == (n, n)
+            sides.add(n)
+    assert 1054 in sides
+    for n in sides:
+        assert _lib.side_supported(n) is not None, n
+    assert _lib.side_supported(1054) == "any" and _lib.side_supported(1024) == "compiled"
