@@ -334,87 +334,6 @@ __device__ __forceinline__ void load_twiddles_pairs(float4* tw, const float2* __
 }
 
 // ---------------------------------------------------------------------------
-// column pass on column pairs: T -> FFT+ (y) -> P_M -> FFT- (y) -> T.
-// A tile is WP pairs of adjacent columns of one individual; thread (h, j)
-// holds the E positions elem_pos(e, j) of pair h.  Columns come straight
-// from HBM as 16-byte pairs (a warp reads row segments of 2 WP columns);
-// with PF the next tile's columns are loaded into registers while the
-// current one is transformed.
-// ---------------------------------------------------------------------------
-template <int N, int WP, bool PF>
-struct PairColCfg {
-  static constexpr int TPT = Plan<N>::TPT;
-  static constexpr int E = Elems<N>::value;
-  static constexpr int W = 2 * WP;
-  static constexpr int NT = WP * TPT;
-  static constexpr int TWB = align128(TwiddleTable<N>::size() * 16);
-  static constexpr int X = align128(ColPairLay<N, WP>::SIZE * 16);
-  static constexpr size_t SMEM = (size_t)TWB + X;
-  static constexpr int REGS = PF ? 128 : 96;
-  static constexpr int MINB_RAW = 65536 / (NT * REGS);
-  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
-};
-
-template <int N, int WP, bool PF>
-__global__ void __launch_bounds__(PairColCfg<N, WP, PF>::NT, PairColCfg<N, WP, PF>::MINB)
-    k_cols_pairs(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count,
-                 const float2* __restrict__ twg) {
-  using C = PairColCfg<N, WP, PF>;
-  constexpr int NT = C::NT, E = C::E, W = C::W, TPI = N / W;
-  using Lay = ColPairLay<N, WP>;
-  extern __shared__ __align__(128) unsigned char sm[];
-  float4* tw = reinterpret_cast<float4*>(sm);
-  float4* xb = reinterpret_cast<float4*>(sm + C::TWB);
-  pdl_enter();
-  load_twiddles_pairs<N>(tw, twg, NT);
-  pdl_wait();
-  __syncthreads();
-  const int t = threadIdx.x;
-  const int h = t % WP, j = t / WP;
-  const int ntiles = count * TPI;
-
-  float4 ct[E];
-  float2 ca[E];
-  auto fetch = [&](int tile) {
-    const int p = first + tile / TPI;
-    const int x = (tile % TPI) * W + 2 * h;
-    const float4* g = reinterpret_cast<const float4*>(T + (size_t)p * N * N + x);
-    const float* Ap = (ipp > 0 ? A + (size_t)(p / ipp) * N * N : A) + x;
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int y = elem_pos<N>(e, j);
-      ct[e] = __ldcs(g + (size_t)y * (N / 2));
-      ca[e] = __ldg(reinterpret_cast<const float2*>(Ap + (size_t)y * N));
-    }
-  };
-
-  int tile = blockIdx.x;
-  if (PF && tile < ntiles) fetch(tile);
-  for (; tile < ntiles; tile += gridDim.x) {
-    if (!PF) fetch(tile);
-    cpair v[E];
-    float2 a[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      v[e] = split2(make_float2(ct[e].x, ct[e].y), make_float2(ct[e].z, ct[e].w));
-      a[e] = ca[e];
-    }
-    const int nxt = tile + gridDim.x;
-    if (PF && nxt < ntiles) fetch(nxt);
-    pfft<N, Lay, +1>(v, xb, tw, h, j);
-#pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = project2(v[e], a[e]);
-    pfft<N, Lay, -1>(v, xb, tw, h, j);
-    const int p = first + tile / TPI;
-    const int x = (tile % TPI) * W + 2 * h;
-    float4* g = reinterpret_cast<float4*>(T + (size_t)p * N * N + x);
-#pragma unroll
-    for (int e = 0; e < E; ++e)
-      g[(size_t)elem_pos<N>(e, j) * (N / 2)] = make_float4(v[e].re.x, v[e].im.x, v[e].re.y, v[e].im.y);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // row pass on row pairs: T -> FFT- (x) -> /N^2 -> update with (rho, S) -> rho
 // -> FFT+ (x) -> T.  A tile is WR pairs of rows (2 WR rows); thread (j, c)
 // holds the positions elem_pos(e, j) of rows 2c and 2c + 1.  The tile's
@@ -517,6 +436,99 @@ __global__ void __launch_bounds__(PairRowCfg<N, WR>::NT, PairRowCfg<N, WR>::MINB
       T[row0 + l] = lane0(v[e]);
       T[row0 + N + l] = lane1(v[e]);
     }
+    __syncthreads();  // stage s is refilled by the next iteration's prefetch
+  }
+}
+
+
+// ---------------------------------------------------------------------------
+// column pass on column pairs: T -> FFT+ (y) -> P_M -> FFT- (y) -> T.  A
+// tile is WP pairs of adjacent columns of one individual; thread (h, j)
+// holds the E positions elem_pos(e, j) of pair h.  The tile's 16-byte column
+// pairs are copied with cp.async one tile ahead, straight into the exchange
+// layout, so that once the first radix pass has read them the stage serves
+// as the exchange buffer (as in k_cols_project); the amplitude columns are
+// staged beside them.
+// ---------------------------------------------------------------------------
+template <int N, int WP>
+struct PairColStCfg {
+  static constexpr int TPT = Plan<N>::TPT;
+  static constexpr int E = Elems<N>::value;
+  static constexpr int W = 2 * WP;
+  static constexpr int NT = WP * TPT;
+  static constexpr int TWB = align128(TwiddleTable<N>::size() * 16);
+  static constexpr int C_T = align128(ColPairLay<N, WP>::SIZE * 16);
+  static constexpr int C_A = align128(N * W * 4);
+  static constexpr int STAGE = C_T + C_A;
+  static constexpr size_t SMEM = (size_t)TWB + 2 * STAGE;
+  static constexpr int MINB_RAW = 65536 / (NT * 104);
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
+};
+
+template <int N, int WP>
+__global__ void __launch_bounds__(PairColStCfg<N, WP>::NT, PairColStCfg<N, WP>::MINB)
+    k_cols_pairs_st(float2* __restrict__ T, const float* __restrict__ A, int ipp, int first, int count,
+                    const float2* __restrict__ twg) {
+  using C = PairColStCfg<N, WP>;
+  constexpr int NT = C::NT, E = C::E, W = C::W, TPI = N / W;
+  using Lay = ColPairLay<N, WP>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  float4* tw = reinterpret_cast<float4*>(sm);
+  unsigned char* stages = sm + C::TWB;
+  pdl_enter();
+  load_twiddles_pairs<N>(tw, twg, NT);
+  pdl_wait();
+  const int t = threadIdx.x;
+  const int h = t % WP, j = t / WP;
+  const int ntiles = count * TPI;
+
+  auto stage_tile = [&](int tile, int s) {
+    const int p = first + tile / TPI;
+    const int x0 = (tile % TPI) * W;
+    float4* sT = reinterpret_cast<float4*>(stages + s * C::STAGE);
+    float* sA = reinterpret_cast<float*>(stages + s * C::STAGE + C::C_T);
+    const float2* gT = T + (size_t)p * N * N + x0;
+    const float* Ap = (ipp > 0 ? A + (size_t)(p / ipp) * N * N : A) + x0;
+    for (int q = t; q < N * WP; q += NT) {  // 16-byte column pairs, a warp per row segment
+      const int y = q / WP, hh = q - y * WP;
+      cp_async16(&sT[Lay::idx(y, hh)], gT + (size_t)y * N + 2 * hh);
+    }
+    for (int q = t; q < N * W / 4; q += NT) {
+      const int y = q / (W / 4), hh = q - y * (W / 4);
+      cp_async16(&sA[y * W + 4 * hh], Ap + (size_t)y * N + 4 * hh);
+    }
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) stage_tile(tile, 0);
+  cp_async_commit();
+  for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) stage_tile(nxt, (k + 1) & 1);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    const int s = k & 1;
+    float4* sT = reinterpret_cast<float4*>(stages + s * C::STAGE);
+    const float* sA = reinterpret_cast<const float*>(stages + s * C::STAGE + C::C_T);
+    cpair v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const float4 t4 = sT[Lay::idx(elem_pos<N>(e, j), h)];  // (re0, im0, re1, im1) as staged
+      v[e] = split2(make_float2(t4.x, t4.y), make_float2(t4.z, t4.w));
+    }
+    __syncthreads();  // the stage's T region becomes the exchange buffer
+    pfft<N, Lay, +1>(v, sT, tw, h, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      v[e] = project2(v[e], *reinterpret_cast<const float2*>(&sA[elem_pos<N>(e, j) * W + 2 * h]));
+    pfft<N, Lay, -1>(v, sT, tw, h, j);
+    const int p = first + tile / TPI;
+    const int x = (tile % TPI) * W + 2 * h;
+    float4* g = reinterpret_cast<float4*>(T + (size_t)p * N * N + x);
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      g[(size_t)elem_pos<N>(e, j) * (N / 2)] = make_float4(v[e].re.x, v[e].im.x, v[e].re.y, v[e].im.y);
     __syncthreads();  // stage s is refilled by the next iteration's prefetch
   }
 }

@@ -128,10 +128,10 @@ template <int N>
 constexpr bool pairs_side_ok() {
   return N == 256 || N == 512 || N == 1024;
 }
-template <int N, int WP, bool PF>
-constexpr bool paircol_ok() {
-  return pairs_side_ok<N>() && WP >= 4 && N % (2 * WP) == 0 && PairColCfg<N, WP, PF>::NT <= 1024 &&
-         PairColCfg<N, WP, PF>::SMEM <= kMaxSmem;
+template <int N, int WP>
+constexpr bool paircolst_ok() {
+  return pairs_side_ok<N>() && WP >= 4 && N % (2 * WP) == 0 && PairColStCfg<N, WP>::NT <= 1024 &&
+         PairColStCfg<N, WP>::SMEM <= kMaxSmem;
 }
 template <int N, int WR>
 constexpr bool pairrow_ok() {
@@ -218,10 +218,10 @@ cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
                     scale, beta, g, c.tw);
 }
 
-template <int N, int WP, bool PF>
-cudaError_t launch_cols_pairs(const Ctx& c) {
-  using P = PairColCfg<N, WP, PF>;
-  auto kern = k_cols_pairs<N, WP, PF>;
+template <int N, int WP>
+cudaError_t launch_cols_pairs_st(const Ctx& c) {
+  using P = PairColStCfg<N, WP>;
+  auto kern = k_cols_pairs_st<N, WP>;
   static std::atomic<unsigned long long> configured{0ull};
   static std::atomic<int> resident[64] = {};
   cudaError_t e = configure(kern, P::SMEM, configured);
@@ -293,16 +293,13 @@ cudaError_t launch_cols_loss(const Ctx& c, float eps, double* partials) {
 // W < 0 two columns per thread, -W columns per tile; 100 + W one warp per
 // column, 200 + W the plan's threads per column (column-major tile, barrier
 // per column), 300 + W one column per thread with the padded layout, W
-// columns per tile; 400 + W column pairs with split real / imaginary parts
-// (spe_pairs.cuh), 500 + W the same with the next tile prefetched into
-// registers
+// columns per tile; 600 + W column pairs with split real / imaginary parts
+// (spe_pairs.cuh), W columns per tile
 template <int N>
 cudaError_t launch_cols_w(const Ctx& c, int w) {
   switch (w) {
-    case 408: if constexpr (paircol_ok<N, 4, false>()) return launch_cols_pairs<N, 4, false>(c); break;
-    case 416: if constexpr (paircol_ok<N, 8, false>()) return launch_cols_pairs<N, 8, false>(c); break;
-    case 508: if constexpr (paircol_ok<N, 4, true>()) return launch_cols_pairs<N, 4, true>(c); break;
-    case 516: if constexpr (paircol_ok<N, 8, true>()) return launch_cols_pairs<N, 8, true>(c); break;
+    case 608: if constexpr (paircolst_ok<N, 4>()) return launch_cols_pairs_st<N, 4>(c); break;
+    case 616: if constexpr (paircolst_ok<N, 8>()) return launch_cols_pairs_st<N, 8>(c); break;
     case 104: if constexpr (warpcol_ok<N, 4>()) return launch_cols_warp<N, 4, 32>(c); break;
     case 108: if constexpr (warpcol_ok<N, 8>()) return launch_cols_warp<N, 8, 32>(c); break;
     case 116: if constexpr (warpcol_ok<N, 16>()) return launch_cols_warp<N, 16, 32>(c); break;
@@ -424,10 +421,8 @@ struct SizeImpl {
 
   static int col_widths(int* out) {
     int k = 0;
-    if constexpr (paircol_ok<N, 4, false>()) out[k++] = 408;
-    if constexpr (paircol_ok<N, 8, false>()) out[k++] = 416;
-    if constexpr (paircol_ok<N, 4, true>()) out[k++] = 508;
-    if constexpr (paircol_ok<N, 8, true>()) out[k++] = 516;
+    if constexpr (paircolst_ok<N, 4>()) out[k++] = 608;
+    if constexpr (paircolst_ok<N, 8>()) out[k++] = 616;
     if constexpr (warpcol_ok<N, 4>()) out[k++] = 104;
     if constexpr (warpcol_ok<N, 8>()) out[k++] = 108;
     if constexpr (warpcol_ok<N, 16>()) out[k++] = 116;

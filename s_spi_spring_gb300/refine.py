@@ -54,13 +54,28 @@ def _bind_stream(engine, device):
     engine.set_stream(h if h else _LEGACY_DEFAULT_STREAM)
 
 
+# gradients up to this size are computed with the loss in the forward pass
+# and kept for the backward; larger ones are recomputed there
+STORE_GRADIENT_BYTES = 4 << 30
+
+
 class FarFieldLoss(torch.autograd.Function):
     """loss[k] = sum over known pixels of the far-field loss of
     support[k] * density[k] (see ``spe_loss_grad``).  Gradient with respect
-    to `density` only (complex autograd convention)."""
+    to `density` only (complex autograd convention).
+
+    With a gradient of at most STORE_GRADIENT_BYTES (or recompute=False) the
+    forward pass computes the loss and the unscaled gradient in one set of
+    passes (rows, columns with the adjoint, rows out) and keeps the gradient;
+    the backward pass only multiplies it by the upstream gradient, or returns
+    it as it is when that is 1 for every item.  Above that size (or with
+    recompute=True) nothing is kept: the backward pass recomputes the
+    transform and applies the adjoint with the upstream scale fused in.  Both
+    give bit-identical gradients (the fused scale multiplies the same values
+    the stored path multiplies, and a scale of 1 is exact)."""
 
     @staticmethod
-    def forward(ctx, density, support, engine, loss="amplitude", eps=0.0):
+    def forward(ctx, density, support, engine, loss="amplitude", eps=0.0, recompute=None):
         if density.dtype != torch.complex64 or not density.is_cuda:
             raise TypeError("density must be a complex64 CUDA tensor")
         density = density.contiguous()
@@ -68,7 +83,16 @@ class FarFieldLoss(torch.autograd.Function):
         count = density.shape[0]
         _bind_stream(engine, density.device)
         out = torch.empty(count, dtype=torch.float64, device=density.device)
-        engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[loss], eps, out.data_ptr(), 0, 0)
+        if recompute is None:
+            recompute = density.numel() * density.element_size() > STORE_GRADIENT_BYTES
+        ctx.grad = None
+        if recompute or not ctx.needs_input_grad[0]:
+            engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[loss], eps, out.data_ptr(), 0, 0)
+        else:
+            grad = torch.empty_like(density)
+            engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[loss], eps, out.data_ptr(),
+                             grad.data_ptr(), 0)
+            ctx.grad = grad
         ctx.save_for_backward(density, support)
         ctx.engine, ctx.loss, ctx.eps = engine, loss, eps
         return out
@@ -78,15 +102,20 @@ class FarFieldLoss(torch.autograd.Function):
         density, support = ctx.saved_tensors
         count = density.shape[0]
         scale = grad_out.to(torch.float32).contiguous()
+        if ctx.grad is not None:
+            grad, ctx.grad = ctx.grad, None
+            if bool(torch.all(scale == 1.0)):
+                return grad, None, None, None, None, None
+            return grad * scale.view(-1, *([1] * (grad.dim() - 1))), None, None, None, None, None
         grad = torch.empty_like(density)
         _bind_stream(ctx.engine, density.device)
         ctx.engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[ctx.loss], ctx.eps, 0,
                              grad.data_ptr(), scale.data_ptr())
-        return grad, None, None, None, None
+        return grad, None, None, None, None, None
 
 
-def farfield_loss(density, support, engine, loss="amplitude", eps=0.0):
-    return FarFieldLoss.apply(density, support, engine, loss, eps)
+def farfield_loss(density, support, engine, loss="amplitude", eps=0.0, recompute=None):
+    return FarFieldLoss.apply(density, support, engine, loss, eps, recompute)
 
 
 def refine(engine, first, count, steps=50, lr=1e-3, loss="poisson", eps=1e-6, device=None, fused=True,

@@ -47,3 +47,23 @@ def test_prtf_matches_restatement():
         assert np.array_equal(a, angles[prof > 0])
         assert np.allclose(p, prof[prof > 0], rtol=1e-4, atol=1e-5)
         assert 0 < p.max() <= 1
+
+
+def test_analysis_matches_the_reference_result_class():
+    """Against the reference's own Result.get_rec_pattern / get_residuals /
+    get_prtf on the same inputs (tests/golden/ref_analysis.npz)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_analysis.npz"))
+    I = g["pattern"]
+    sol = Solver(I, gpus=[0], seed=1)
+    recs = [Reconstruction(g["density"][k], g["support"]) for k in range(g["density"].shape[0])]
+    rp = analysis.rec_patterns(sol, recs)
+    res = analysis.residuals(sol, I, recs)
+    pr = analysis.prtf(sol, I, recs)
+    for k in range(len(recs)):
+        ref = g[f"rec_pattern_{k}"]
+        assert np.abs(rp[k] - ref).max() <= 1e-5 * ref.max()
+        assert np.abs(res[k] - g[f"residuals_{k}"]).max() <= 1e-5 * ref.max()
+        a, p = pr[k]
+        assert np.array_equal(a, g[f"prtf_angles_{k}"])
+        assert np.allclose(p, g[f"prtf_{k}"], rtol=1e-4, atol=1e-5)

@@ -126,3 +126,24 @@ def test_fused_adam_matches_autograd_adam(loss):
     assert np.linalg.norm(da - db) <= 1e-4 * np.linalg.norm(db)
     assert np.array_equal(da[S == 0], dens[S == 0])
     assert ha[-1] < ha[0]
+
+
+@pytest.mark.parametrize("loss,eps", [("amplitude", 0.0), ("poisson", 1e-3)])
+def test_stored_and_recomputed_gradients_are_bit_identical(loss, eps):
+    """FarFieldLoss computes the gradient with the loss and keeps it (small
+    sizes), or recomputes it in the backward pass with the upstream scale
+    fused (large sizes): the same bits either way, with unit and non-unit
+    upstream gradients."""
+    n, P = 128, 3
+    eng, A, dens, S = setup(n, P, seed=21)
+    s = torch.tensor(S, device=DEV)
+    for weights in (None, np.array([1.0, 0.5, 2.0])):
+        out = []
+        for recompute in (False, True):
+            d = torch.tensor(dens, device=DEV, requires_grad=True)
+            L = FarFieldLoss.apply(d, s, eng, loss, eps, recompute)
+            w = torch.ones_like(L) if weights is None else torch.tensor(weights, device=DEV, dtype=torch.float64)
+            (L * w).sum().backward()
+            out.append((L.detach().cpu().numpy(), d.grad.cpu().numpy()))
+        assert np.array_equal(out[0][0], out[1][0])
+        assert np.array_equal(out[0][1].view(np.uint32), out[1][1].view(np.uint32))
