@@ -518,8 +518,9 @@ def large_memetic(args, local):
     generations: 2048 x 2048, 128 individuals; per generation shrink-wrap,
     alignment, average, crossover, the sequences on parents and children
     (RAAR beta 0.87, 200 iterations per main step, ER, shrink-wrap sigma 3 ->
-    1.5 at threshold 0.1) and 20 fused Adam steps of gradient refinement on
-    parents and children before the replacement; the error sums in FP64.
+    1.5 at threshold 0.1) and 20 fused Adam steps of gradient refinement
+    (Poisson loss, step 5e-5) on parents and children before the
+    replacement; the error sums in FP64.
     Reports seconds per generation, the iterations run, the best R-factor,
     and the reconstruction error of the best individual against the true
     object after the reference's alignment (translation, global phase, twin;
@@ -530,8 +531,11 @@ def large_memetic(args, local):
     from s_spi_spring_gb300.spring_core.phase_retrieval import Solver
     n, P = 2048, 128
     I, obj, _ = synthetic.ellipsoid_cluster_pattern(seed=9, n=n, extent=480.0, photons=1e9, masked=0.25)
+    # the refinement step is relative to the densities' scale (about 0.05 at
+    # most here: a start scaled to the pattern's power), so that 20 Adam
+    # steps move a pixel by at most a few per cent of it
     st = MemeticSettings(generations=20, popsize=P, alg="RAAR", it=200, beta=BETA, it_ER=40, it_eval=40, sigma=3.0,
-                         threshold=0.1, refine_steps=20)
+                         threshold=0.1, refine_steps=20, refine_lr=5e-5)
     sol = Solver(I, gpus=[local], seed=42)
     recs = sol.InitializePop(P, 600, itemsize=[120.0, 540.0], nitems=[2, 8], exponent=[0.5, 0.5], scaling=[0.5, 1.5],
                              phaserange=0)

@@ -231,7 +231,22 @@ spe::Ctx make_ctx(spe_engine* e, int first, int count) {
   c.grid_div = 1;
   c.mark = nullptr;
   c.ipp = e->ipp;
+  c.tma = e->tma;
+  c.err = e->dev_err;
   return c;
+}
+
+// A bounded wait that gave up on the device (the TMA row pass) leaves its
+// flag set: reported at the next point where the host waits for the engine.
+int check_device_flag(spe_engine* e) {
+  if (!e->dev_err) return SPE_OK;
+  int flag = 0;
+  CK(cudaMemcpy(&flag, e->dev_err, sizeof(int), cudaMemcpyDeviceToHost), "device flag");
+  if (flag) {
+    CK(cudaMemset(e->dev_err, 0, sizeof(int)), "device flag");
+    return fail(SPE_ERR_CUDA, "a kernel's bounded wait for its tile copies timed out (TMA row pass)");
+  }
+  return SPE_OK;
 }
 
 int pattern_of_range(spe_engine* e, int first, int count, const float** A) {
@@ -482,6 +497,8 @@ int spe_create(int n, int device, spe_engine** out) {
   err = cudaMalloc(&e->tw, tw.size() * sizeof(float2));
   if (err == cudaSuccess) err = cudaMalloc(&e->A, e->npix * sizeof(float));
   if (err == cudaSuccess) err = cudaMemcpy(e->tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMalloc(&e->dev_err, sizeof(int));
+  if (err == cudaSuccess) err = cudaMemset(e->dev_err, 0, sizeof(int));
   // a pageable host-to-device cudaMemcpy may return before the data has
   // landed, and nothing orders it before kernels on the engine's
   // non-blocking stream (which read the twiddles before griddepcontrol.wait)
@@ -489,6 +506,7 @@ int spe_create(int n, int device, spe_engine** out) {
   if (err != cudaSuccess) {
     cudaFree(e->tw);
     cudaFree(e->A);
+    cudaFree(e->dev_err);
     cudaStreamDestroy(e->own);
     delete e;
     return cuda_fail(err, "engine allocation");
@@ -504,6 +522,8 @@ int spe_destroy(spe_engine* e) {
   free_population(e);
   cudaFree(e->A);
   cudaFree(e->tw);
+  cudaFree(e->dev_err);
+  delete[] static_cast<unsigned char*>(e->tma);
   cudaFree(e->avg_mod);
   cudaFree(e->ref);
   cudaFree(e->work);
@@ -616,6 +636,16 @@ int spe_reserve(spe_engine* e, int capacity) {
   e->rho = t.rho;
   e->S = t.S;
   e->T = t.T;
+  {  // the TMA row pass's tensor maps describe these arrays
+    unsigned char* maps = static_cast<unsigned char*>(e->tma);
+    if (!maps) maps = new unsigned char[spe::row_maps_bytes()];
+    if (spe::build_row_maps(maps, e->n, e->cap, t.T, t.rho, t.S)) {
+      e->tma = maps;
+    } else {
+      delete[] maps;
+      e->tma = nullptr;
+    }
+  }
   e->T2 = t.T2;
   e->M = t.M;
   e->partials = t.partials;
@@ -656,7 +686,7 @@ int spe_download(spe_engine* e, int first, int count, float* density, int32_t* s
   if (support && count)
     CK(cudaMemcpyAsync(support, e->S + off, np * sizeof(int), cudaMemcpyDeviceToHost, e->st), "download support");
   CK(cudaStreamSynchronize(e->st), "synchronize");
-  return SPE_OK;
+  return check_device_flag(e);
 }
 
 int spe_device_buffers(spe_engine* e, void** density, void** support) {
@@ -1087,7 +1117,7 @@ int spe_synchronize(spe_engine* e) {
   if (!e) return fail(SPE_ERR_INVALID, "null engine");
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   CK(cudaStreamSynchronize(e->st), "synchronize");
-  return SPE_OK;
+  return check_device_flag(e);
 }
 
 }  // extern "C"

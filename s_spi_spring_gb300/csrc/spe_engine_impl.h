@@ -47,6 +47,8 @@ struct spe_engine {
   // (ipp = 0: one pattern for every slot)
   int npatterns = 1, ipp = 0;
   int a_cap = 1;  // patterns the A allocation holds
+  void* tma = nullptr;     // tensor maps of the TMA row pass (null: not available)
+  int* dev_err = nullptr;  // device flag of the kernels' bounded waits
   cudaStream_t lane2 = nullptr;          // second lane (created on first use)
   cudaEvent_t fork = nullptr, join = nullptr, phase = nullptr;
 };

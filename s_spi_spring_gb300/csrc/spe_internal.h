@@ -58,7 +58,17 @@ struct Ctx {
   int grid_div;         // persistent kernels use 1/grid_div of the resident CTAs (<= 1: all)
   cudaEvent_t mark;     // if set, recorded after the first column pass of an iteration call
   int ipp;              // individuals per pattern (slot p uses pattern p / ipp of A); 0: A is one pattern
+  const void* tma;      // tensor maps of the TMA row pass (row_maps), or null
+  int* err;             // device flag set by a bounded wait that gave up, or null
 };
+
+// Tensor maps of the TMA row pass (spe_tma_maps.cu): row_maps_bytes() of
+// storage holding one set of maps (T, rho, S) per row-tile width 1, 2, 4, 8.
+// build_row_maps fills them for population arrays of `cap` individuals of
+// side n; false when the side has no TMA row pass or the driver lacks
+// cuTensorMapEncodeTiled.
+size_t row_maps_bytes();
+bool build_row_maps(void* out, int n, int cap, const float2* T, const float2* rho, const int* S);
 
 // Phase gate (see phase_out in spe_kernels.cuh): float thresholds of
 // arg > hi / arg < -lo and the cos / sin of each threshold.

@@ -13,14 +13,16 @@
 // columns) of one individual in shared memory, applies the operation's load,
 // transforms, pointwise step and store (the same op functors as the
 // compiled passes), and reduces its partial sums.  The 1D transform is a
-// self-sorting Stockham FFT over the prime factors of the side (radix 4 where
-// the side has a factor 4): every pass computes each output as the direct
-// sum over its radix-R inputs with the combined twiddle
+// self-sorting Stockham FFT over the factors of the side (radix 8, then 4,
+// then the primes), with the twiddles of a table exp(2 pi i m / n) computed
+// in double and held in shared memory.  Radices 2, 3, 4, 5, 7 and 8 run as
+// butterflies in registers (a thread reads the R inputs of one butterfly,
+// applies its twiddles and the radix-R DFT, writes R outputs); a larger prime
+// radix computes each output as the direct sum over its R inputs with the
+// combined twiddle
 //   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)),
-// k = b mod NS, from a table exp(2 pi i m / n) computed in double.  A pass
-// costs R complex multiply-adds per point, so a side with a large prime
-// factor p costs p per point: sides whose largest prime factor exceeds
-// kMaxPrime are rejected rather than run at that cost.
+// k = b mod NS, R complex multiply-adds per point: sides whose largest prime
+// factor exceeds kMaxPrime are rejected rather than run at that cost.
 #include <map>
 #include <memory>
 #include <mutex>
@@ -43,37 +45,117 @@ struct AnyPlan {
   int rad[kMaxRadices];   // radices in pass order
 };
 
-// out[c * LS + pos] for the W lines of the tile: one radix pass per factor,
-// ping-ponging between the two line buffers.  On return `cur` holds the
-// transform.
+// Radix-R DFT of R registers with compile-time twiddles, R = 5 or 7 (the
+// other radices of the butterfly passes use dft<R, S> of spe_fft.cuh):
+// v[q] <- sum_r v[r] exp(S 2 pi i r q / R)
+template <int R, int S, int Q, int RR>
+__device__ __forceinline__ void dft_direct_term(const float2* x, float2& acc) {
+  if constexpr (RR < R) {
+    const float2 t = ctwiddle<S, RR * Q, R>(x[RR]);
+    acc = make_float2(acc.x + t.x, acc.y + t.y);
+    dft_direct_term<R, S, Q, RR + 1>(x, acc);
+  }
+}
+template <int R, int S, int Q>
+__device__ __forceinline__ void dft_direct_out(const float2* x, float2* v) {
+  if constexpr (Q < R) {
+    float2 acc = x[0];
+    dft_direct_term<R, S, Q, 1>(x, acc);
+    v[Q] = acc;
+    dft_direct_out<R, S, Q + 1>(x, v);
+  }
+}
+template <int R, int S>
+__device__ __forceinline__ void small_dft(float2* v) {
+  if constexpr (R == 5 || R == 7) {
+    float2 x[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) x[r] = v[r];
+    dft_direct_out<R, S, 0>(x, v);
+  } else {
+    dft<R, S>(v);
+  }
+}
+
+// One Stockham pass of radix R as butterflies: each thread reads the R
+// inputs x[b + r n/R] of a butterfly, multiplies them by w_{NS R}^{k r}
+// (k = b mod NS), runs the radix-R DFT in registers and writes its R
+// outputs at (b/NS) NS R + k + q NS.
+template <int R, int S>
+__device__ __forceinline__ void any_pass_r(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw, int nl,
+                                           int NS) {
+  const int n = pl.n, LS = pl.LS, m = n / R, tstep = n / (NS * R);
+  for (int i = threadIdx.x; i < nl * m; i += kAnyThreads) {
+    const int c = i / m, b = i - c * m;
+    const int k = b % NS;
+    const float2* src = cur + c * LS + b;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[r * m];
+    if (NS > 1) {
+      const int e = k * tstep;  // < n / R
+      int idx = 0;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        idx += e;
+        float2 w = tw[idx];
+        if (S < 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    small_dft<R, S>(v);
+    float2* dst = oth + c * LS + (b / NS) * NS * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) dst[q * NS] = v[q];
+  }
+}
+
+// One pass of any other (prime) radix: each output as the direct sum over
+// its R inputs with the combined twiddle
+//   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)).
 template <int S>
-__device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPlan& pl,
-                                        const float2* __restrict__ tw, int nl) {
+__device__ __forceinline__ void any_pass_generic(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw,
+                                                 int nl, int NS, int R) {
   const int n = pl.n, LS = pl.LS;
+  const int m = n / R;        // butterflies; input stride
+  const int span = NS * R;    // outputs of one sub-transform
+  const int tstep = n / span; // twiddle-table step of one unit of (k + q NS)
+  for (int i = threadIdx.x; i < nl * n; i += kAnyThreads) {
+    const int c = i / n, pos = i - c * n;
+    const int j = pos / span, rem = pos - j * span;
+    const int q = rem / NS, k = rem - q * NS;
+    const float2* src = cur + c * LS + j * NS + k;
+    const int e = (k + q * NS) * tstep;  // < n
+    float2 acc = src[0];
+    int idx = 0;
+    for (int r = 1; r < R; ++r) {
+      idx += e;
+      if (idx >= n) idx -= n;
+      float2 w = tw[idx];
+      if (S < 0) w.y = -w.y;
+      const float2 x = src[r * m];
+      acc.x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc.x));
+      acc.y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc.y));
+    }
+    oth[c * LS + pos] = acc;
+  }
+}
+
+// The transform of the tile's nl lines: one pass per radix of the plan,
+// ping-ponging between the two line buffers; on return `cur` holds it.
+template <int S>
+__device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPlan& pl, const float2* tw, int nl) {
   int NS = 1;
   for (int ps = 0; ps < pl.nrad; ++ps) {
     const int R = pl.rad[ps];
-    const int m = n / R;        // butterflies; input stride
-    const int span = NS * R;    // outputs of one sub-transform
-    const int tstep = n / span; // twiddle-table step of one unit of (k + q NS)
-    for (int i = threadIdx.x; i < nl * n; i += kAnyThreads) {
-      const int c = i / n, pos = i - c * n;
-      const int j = pos / span, rem = pos - j * span;
-      const int q = rem / NS, k = rem - q * NS;
-      const float2* src = cur + c * LS + j * NS + k;
-      const int e = (k + q * NS) * tstep;  // < n
-      float2 acc = src[0];
-      int idx = 0;
-      for (int r = 1; r < R; ++r) {
-        idx += e;
-        if (idx >= n) idx -= n;
-        float2 w = __ldg(tw + idx);
-        if (S < 0) w.y = -w.y;
-        const float2 x = src[r * m];
-        acc.x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc.x));
-        acc.y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc.y));
-      }
-      oth[c * LS + pos] = acc;
+    switch (R) {
+      case 2: any_pass_r<2, S>(cur, oth, pl, tw, nl, NS); break;
+      case 3: any_pass_r<3, S>(cur, oth, pl, tw, nl, NS); break;
+      case 4: any_pass_r<4, S>(cur, oth, pl, tw, nl, NS); break;
+      case 5: any_pass_r<5, S>(cur, oth, pl, tw, nl, NS); break;
+      case 7: any_pass_r<7, S>(cur, oth, pl, tw, nl, NS); break;
+      case 8: any_pass_r<8, S>(cur, oth, pl, tw, nl, NS); break;
+      default: any_pass_generic<S>(cur, oth, pl, tw, nl, NS, R); break;
     }
     __syncthreads();
     float2* t = cur;
@@ -89,6 +171,8 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
   const int n = pl.n, W = pl.W, LS = pl.LS;
   float2* cur = sm_any;
   float2* oth = sm_any + (size_t)W * LS;
+  float2* tws = sm_any + (size_t)2 * W * LS;  // the twiddle table, n entries
+  for (int i = threadIdx.x; i < n; i += kAnyThreads) tws[i] = __ldg(tw + i);
   const int tpi = (n + W - 1) / W;
   const int p = op.first + blockIdx.x / tpi;
   const int l0 = (blockIdx.x % tpi) * W;
@@ -117,7 +201,7 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
     cur[c * LS + l] = op.load(base + (size_t)y * n + x, p, y, x, acc);
   }
   __syncthreads();
-  if constexpr (Op::FFT1 != 0) fft_any<Op::FFT1>(cur, oth, pl, tw, nl);
+  if constexpr (Op::FFT1 != 0) fft_any<Op::FFT1>(cur, oth, pl, tws, nl);
   if constexpr (Op::FFT2 != 0) {
     for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
       int c, l, y, x;
@@ -125,7 +209,7 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
       cur[c * LS + l] = op.mid(cur[c * LS + l], base + (size_t)y * n + x, p, y, x, acc);
     }
     __syncthreads();
-    fft_any<Op::FFT2>(cur, oth, pl, tw, nl);
+    fft_any<Op::FFT2>(cur, oth, pl, tws, nl);
   }
   for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
     int c, l, y, x;
@@ -148,6 +232,10 @@ bool make_plan(int n, AnyPlan& pl) {
   pl.n = n;
   pl.nrad = 0;
   int m = n;
+  while (m % 8 == 0 && pl.nrad < kMaxRadices) {
+    pl.rad[pl.nrad++] = 8;
+    m /= 8;
+  }
   while (m % 4 == 0 && pl.nrad < kMaxRadices) {
     pl.rad[pl.nrad++] = 4;
     m /= 4;
@@ -163,9 +251,10 @@ bool make_plan(int n, AnyPlan& pl) {
   }
   if (m != 1) return false;
   pl.LS = n | 1;
+  const size_t table = (size_t)n * sizeof(float2);
   const size_t per_line = 2 * (size_t)pl.LS * sizeof(float2);
-  const size_t w = kAnySmem / per_line;
-  if (w < 1) return false;
+  if (table + per_line > kAnySmem) return false;
+  const size_t w = (kAnySmem - table) / per_line;
   pl.W = (int)(w < 8 ? w : 8);
   return true;
 }
@@ -183,7 +272,7 @@ const AnyPlan& plan_of(int n) {
   return g_any.at(n)->plan;
 }
 
-size_t smem_of(const AnyPlan& pl) { return 2 * (size_t)pl.W * pl.LS * sizeof(float2); }
+size_t smem_of(const AnyPlan& pl) { return (2 * (size_t)pl.W * pl.LS + pl.n) * sizeof(float2); }
 
 template <int AXIS, class Op>
 cudaError_t launch_any(const Op& op, const AnyPlan& pl, int count, cudaStream_t st, const float2* tw) {

@@ -7,6 +7,7 @@
 #include "spe_kernels.cuh"
 #include "spe_pipe.cuh"
 #include "spe_pairs.cuh"
+#include "spe_tma.cuh"
 
 namespace spe {
 
@@ -133,6 +134,13 @@ constexpr bool paircolst_ok() {
   return pairs_side_ok<N>() && WP >= 4 && N % (2 * WP) == 0 && PairColStCfg<N, WP>::NT <= 1024 &&
          PairColStCfg<N, WP>::SMEM <= kMaxSmem;
 }
+// TMA row pass (spe_tma.cuh): sides 256, 512, 1024 (whose tensor maps the
+// engine builds), W = 2, 4, 8 rows per tile
+template <int N, int W, class XLay>
+constexpr bool tmarow_ok() {
+  return (N == 256 || N == 512 || N == 1024) && N % W == 0 && TmaRowCfg<N, W, XLay>::NT % 32 == 0 &&
+         TmaRowCfg<N, W, XLay>::NT <= 1024 && TmaRowCfg<N, W, XLay>::SMEM <= kMaxSmem;
+}
 template <int N, int WR>
 constexpr bool pairrow_ok() {
   return pairs_side_ok<N>() && N % (2 * WR) == 0 && PairRowCfg<N, WR>::NT % 32 == 0 &&
@@ -232,6 +240,24 @@ cudaError_t launch_cols_pairs_st(const Ctx& c) {
   return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.A, c.ipp, c.first, c.count, c.tw);
 }
 
+template <int N, int W, int UPD, class XLay>
+cudaError_t launch_rows_tma(const Ctx& c, float scale, float beta, Gate g) {
+  if (!c.tma || !c.err) return cudaErrorInvalidValue;  // no tensor maps for these arrays
+  using P = TmaRowCfg<N, W, XLay>;
+  auto kern = k_rows_tma<N, W, UPD, XLay>;
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / W);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
+  const int grid = tiles < slots ? tiles : slots;
+  constexpr int slot = W == 1 ? 0 : (W == 2 ? 1 : (W == 4 ? 2 : 3));
+  const RowMaps& maps = static_cast<const RowMaps*>(c.tma)[slot];
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, maps, c.T, c.rho, c.first, c.count, scale, beta, g, c.tw,
+                    c.err);
+}
+
 template <int N, int WR, int UPD>
 cudaError_t launch_rows_pairs(const Ctx& c, float scale, float beta, Gate g) {
   using P = PairRowCfg<N, WR>;
@@ -318,12 +344,19 @@ cudaError_t launch_cols_w(const Ctx& c, int w) {
   return cudaErrorInvalidValue;
 }
 
-// row-pass variant code: W rows per tile, one row per W threads groups;
-// 100 + W the per-exchange padding; 400 + W row pairs with split real /
-// imaginary parts (spe_pairs.cuh)
+// row-pass variant code: W rows per tile; 100 + W the per-exchange
+// padding; 400 + W row pairs with split real / imaginary parts
+// (spe_pairs.cuh); 500 + W / 600 + W tiles moved by the TMA (spe_tma.cuh)
+// with the plain / the per-exchange padding
 template <int N, int UPD>
 cudaError_t launch_rows_w(const Ctx& c, int w, float scale, float beta, Gate g) {
   switch (w) {
+    case 502: if constexpr (tmarow_ok<N, 2, LayPad<N, 2>>()) return launch_rows_tma<N, 2, UPD, LayPad<N, 2>>(c, scale, beta, g); break;
+    case 504: if constexpr (tmarow_ok<N, 4, LayPad<N, 4>>()) return launch_rows_tma<N, 4, UPD, LayPad<N, 4>>(c, scale, beta, g); break;
+    case 508: if constexpr (tmarow_ok<N, 8, LayPad<N, 8>>()) return launch_rows_tma<N, 8, UPD, LayPad<N, 8>>(c, scale, beta, g); break;
+    case 602: if constexpr (RowPads<N>::n > 0 && tmarow_ok<N, 2, LayRowX<N, 2>>()) return launch_rows_tma<N, 2, UPD, LayRowX<N, 2>>(c, scale, beta, g); break;
+    case 604: if constexpr (RowPads<N>::n > 0 && tmarow_ok<N, 4, LayRowX<N, 4>>()) return launch_rows_tma<N, 4, UPD, LayRowX<N, 4>>(c, scale, beta, g); break;
+    case 608: if constexpr (RowPads<N>::n > 0 && tmarow_ok<N, 8, LayRowX<N, 8>>()) return launch_rows_tma<N, 8, UPD, LayRowX<N, 8>>(c, scale, beta, g); break;
     case 402: if constexpr (pairrow_ok<N, 1>()) return launch_rows_pairs<N, 1, UPD>(c, scale, beta, g); break;
     case 404: if constexpr (pairrow_ok<N, 2>()) return launch_rows_pairs<N, 2, UPD>(c, scale, beta, g); break;
     case 408: if constexpr (pairrow_ok<N, 4>()) return launch_rows_pairs<N, 4, UPD>(c, scale, beta, g); break;
@@ -440,6 +473,12 @@ struct SizeImpl {
   }
   static int row_widths(int* out) {
     int k = 0;
+    if constexpr (tmarow_ok<N, 2, LayPad<N, 2>>()) out[k++] = 502;
+    if constexpr (tmarow_ok<N, 4, LayPad<N, 4>>()) out[k++] = 504;
+    if constexpr (tmarow_ok<N, 8, LayPad<N, 8>>()) out[k++] = 508;
+    if constexpr (RowPads<N>::n > 0 && tmarow_ok<N, 2, LayRowX<N, 2>>()) out[k++] = 602;
+    if constexpr (RowPads<N>::n > 0 && tmarow_ok<N, 4, LayRowX<N, 4>>()) out[k++] = 604;
+    if constexpr (RowPads<N>::n > 0 && tmarow_ok<N, 8, LayRowX<N, 8>>()) out[k++] = 608;
     if constexpr (pairrow_ok<N, 1>()) out[k++] = 402;
     if constexpr (pairrow_ok<N, 2>()) out[k++] = 404;
     if constexpr (pairrow_ok<N, 4>()) out[k++] = 408;

@@ -67,8 +67,8 @@ class FarFieldLoss(torch.autograd.Function):
     With a gradient of at most STORE_GRADIENT_BYTES (or recompute=False) the
     forward pass computes the loss and the unscaled gradient in one set of
     passes (rows, columns with the adjoint, rows out) and keeps the gradient;
-    the backward pass only multiplies it by the upstream gradient, or returns
-    it as it is when that is 1 for every item.  Above that size (or with
+    the backward pass only multiplies it by the upstream gradient (one
+    elementwise pass).  Above that size (or with
     recompute=True) nothing is kept: the backward pass recomputes the
     transform and applies the adjoint with the upstream scale fused in.  Both
     give bit-identical gradients (the fused scale multiplies the same values
@@ -104,9 +104,12 @@ class FarFieldLoss(torch.autograd.Function):
         scale = grad_out.to(torch.float32).contiguous()
         if ctx.grad is not None:
             grad, ctx.grad = ctx.grad, None
-            if bool(torch.all(scale == 1.0)):
-                return grad, None, None, None, None, None
-            return grad * scale.view(-1, *([1] * (grad.dim() - 1))), None, None, None, None, None
+            # real and imaginary parts scaled separately, in place, as the
+            # kernel does (a complex-by-real product in torch would add +-0
+            # terms and turn -0 into +0); no host check of the scale, which
+            # would wait for the device
+            torch.view_as_real(grad).mul_(scale.view(-1, *([1] * grad.dim())))
+            return grad, None, None, None, None, None
         grad = torch.empty_like(density)
         _bind_stream(ctx.engine, density.device)
         ctx.engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[ctx.loss], ctx.eps, 0,

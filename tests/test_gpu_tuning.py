@@ -33,7 +33,8 @@ def test_all_tile_widths_bit_identical(n):
     ref = None
     tried = 0
     for wc, wr in itertools.product([4, 8, 16, -4, -8, -16, 104, 108, 116, 204, 208, 304, 308, 608, 616],
-                                    [1, 2, 4, 8, 16, 101, 102, 104, 108, 402, 404, 408]):
+                                    [1, 2, 4, 8, 16, 101, 102, 104, 108, 402, 404, 408, 502, 504, 508, 602, 604,
+                                     608]):
         try:
             e.set_tiles(wc, wr)
         except _lib.EngineError:
