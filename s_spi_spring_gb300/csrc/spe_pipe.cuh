@@ -390,6 +390,102 @@ __global__ void __launch_bounds__(RowCfg<N, W, XLay>::NT, RowCfg<N, W, XLay>::MI
 }
 
 // ---------------------------------------------------------------------------
+// Row passes of the far-field loss and its adjoint, persistent and staged like
+// k_rows_iterate (the same per-element arithmetic as the pass_kernel ops
+// OpRowsSupportForward and OpRowsGradOut, so the results are bit-identical):
+//   ROWS_SUPPORT_FORWARD: (S > 0 ? src : 0) -> FFT+ (x) -> dst
+//   ROWS_GRAD_OUT:        src -> FFT- (x) -> dst = f * (.), f = S > 0 ? scale[p - first] (1 without scale) : 0
+// A tile's rows of src and S are staged with cp.async one tile ahead.
+// ---------------------------------------------------------------------------
+enum { ROWS_SUPPORT_FORWARD = 0, ROWS_GRAD_OUT = 1 };
+
+template <int N, int W>
+struct RowsIoCfg {  // W rows per tile, src (complex) and S staged
+  static constexpr int TPT = Plan<N>::TPT;
+  static constexpr int E = Elems<N>::value;
+  static constexpr int TWB = align128(TwiddleTable<N>::size() * 8);
+  static constexpr int NT = W * TPT;
+  static constexpr int R_D = align128(N * W * 8);
+  static constexpr int R_S = align128(N * W * 4);
+  static constexpr int STAGE = R_D + R_S;
+  static constexpr int R_X = align128(LayPad<N, W>::SIZE * 8);
+  static constexpr size_t SMEM = (size_t)TWB + R_X + 2 * STAGE;
+  static constexpr int MINB_RAW = 65536 / (NT * (E <= 8 ? 80 : 128));
+  static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
+};
+
+template <int N, int W, int MODE>
+__global__ void __launch_bounds__(RowsIoCfg<N, W>::NT, RowsIoCfg<N, W>::MINB)
+    k_rows_io(const float2* __restrict__ src, const int* __restrict__ S, float2* __restrict__ dst,
+              const float* __restrict__ scale, int first, int count, const float2* __restrict__ twg) {
+  using C = RowsIoCfg<N, W>;
+  constexpr int NT = C::NT, E = C::E, TPT = C::TPT, TPI = N / W;
+  using Lay = LayPad<N, W>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  float2* tw = reinterpret_cast<float2*>(sm);
+  float2* xb = reinterpret_cast<float2*>(sm + C::TWB);
+  unsigned char* stages = sm + C::TWB + C::R_X;
+  pdl_enter();
+  load_twiddles<N>(tw, twg, NT);
+  pdl_wait();
+  const int t = threadIdx.x;
+  const int j = t % TPT, c = t / TPT;
+  const int ntiles = count * TPI;
+
+  auto stage_tile = [&](int tile, int s) {
+    const int p = first + tile / TPI;
+    const int y0 = (tile % TPI) * W;
+    const size_t base = (size_t)p * N * N + (size_t)y0 * N;
+    unsigned char* st = stages + s * C::STAGE;
+    float2* sD = reinterpret_cast<float2*>(st);
+    int* sS = reinterpret_cast<int*>(st + C::R_D);
+    for (int q = t; q < N * W / 2; q += NT) cp_async16(&sD[2 * q], src + base + 2 * q);
+    for (int q = t; q < N * W / 4; q += NT) cp_async16(&sS[4 * q], S + base + 4 * q);
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) stage_tile(tile, 0);
+  cp_async_commit();
+  for (int k = 0; tile < ntiles; ++k, tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) stage_tile(nxt, (k + 1) & 1);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    const int s = k & 1;
+    const unsigned char* st = stages + s * C::STAGE;
+    const float2* sD = reinterpret_cast<const float2*>(st);
+    const int* sS = reinterpret_cast<const int*>(st + C::R_D);
+    const int p = first + tile / TPI;
+    const int y = (tile % TPI) * W + c;
+    const size_t rowbase = (size_t)p * N * N + (size_t)y * N;
+    float2 v[E];
+    if constexpr (MODE == ROWS_SUPPORT_FORWARD) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int l = elem_pos<N>(e, j);
+        v[e] = sS[c * N + l] > 0 ? sD[c * N + l] : make_float2(0.f, 0.f);
+      }
+      fft_reg<N, Lay, +1>(v, xb, tw, c, j);
+#pragma unroll
+      for (int e = 0; e < E; ++e) dst[rowbase + elem_pos<N>(e, j)] = v[e];
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = sD[c * N + elem_pos<N>(e, j)];
+      fft_reg<N, Lay, -1>(v, xb, tw, c, j);
+      const float sp = scale ? scale[p - first] : 1.f;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int l = elem_pos<N>(e, j);
+        const float f = sS[c * N + l] > 0 ? sp : 0.f;
+        dst[rowbase + l] = make_float2(v[e].x * f, v[e].y * f);
+      }
+    }
+    __syncthreads();  // stage s is refilled by the next iteration's prefetch
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Column pass with two columns per thread.  Thread (pair h, j) holds the E
 // elements of columns 2h and 2h+1 at the same positions, so every exchange
 // moves one 16-byte (float4) element pair, each twiddle loaded serves both

@@ -197,6 +197,35 @@ inline int share(int slots, int div) {
   return s < 1 ? 1 : s;
 }
 
+// persistent staged row passes of the loss (k_rows_io): sides from 256, the
+// default row-tile width
+template <int N>
+constexpr int rowsio_w() {
+  return DefaultTiles<N>::rows;
+}
+template <int N>
+constexpr bool rowsio_ok() {
+  constexpr int W = rowsio_w<N>();
+  return N >= 256 && N % W == 0 && RowsIoCfg<N, W>::NT % 32 == 0 && RowsIoCfg<N, W>::NT <= 1024 &&
+         RowsIoCfg<N, W>::SMEM <= kMaxSmem;
+}
+template <int N, int MODE>
+cudaError_t launch_rows_io(const Ctx& c, const float2* src, float2* dst, const float* scale) {
+  constexpr int W = rowsio_w<N>();
+  using P = RowsIoCfg<N, W>;
+  auto kern = k_rows_io<N, W, MODE>;
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / W);
+  const int slots = resident_ctas(kern, P::NT, P::SMEM, resident);
+  const int grid = tiles < slots ? tiles : slots;
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, src, static_cast<const int*>(c.S), dst, scale, c.first,
+                    c.count, c.tw);
+}
+
+
 template <int N, int W, class Lay = LayCol<N, W>>
 cudaError_t launch_cols_project(const Ctx& c) {
   using P = ColCfg<N, W, Lay>;
@@ -689,38 +718,45 @@ struct SizeImpl {
   // far-field loss per item into partials (column-pass tiles); with grad,
   // grad = scale[p] * 2 S FFT-(dL/dconj F) for items [first, first+count)
   // of c.rho / c.S (c.T is scratch)
+  // S * rho -> FFT+ (x) -> T: the staged persistent pass where compiled
+  static cudaError_t support_forward(const Ctx& c) {
+    if constexpr (rowsio_ok<N>()) {
+      return launch_rows_io<N, ROWS_SUPPORT_FORWARD>(c, c.rho, c.T, nullptr);
+    } else {
+      OpRowsSupportForward rf;
+      rf.first = c.first;
+      rf.partials = nullptr;
+      rf.rho = c.rho;
+      rf.S = c.S;
+      rf.T = c.T;
+      return launch_pass<N, AX_ROWS>(rf, c.count, c.st, c.tw);
+    }
+  }
+
   template <int LOSS>
   static cudaError_t loss_grad_t(const Ctx& c, float eps, double* partials, float2* grad, const float* scale) {
-    OpRowsSupportForward rf;
-    rf.first = c.first;
-    rf.partials = nullptr;
-    rf.rho = c.rho;
-    rf.S = c.S;
-    rf.T = c.T;
-    SPE_TRY((launch_pass<N, AX_ROWS>(rf, c.count, c.st, c.tw)));
+    SPE_TRY(support_forward(c));
     constexpr int WL = DefaultTiles<N>::cols;  // loss partials: N / WL per item
     if (!grad) return launch_cols_loss<N, WL, LOSS, false>(c, eps, partials);
     SPE_TRY((launch_cols_loss<N, WL, LOSS, true>(c, eps, partials)));
-    OpRowsGradOut go;
-    go.first = c.first;
-    go.partials = nullptr;
-    go.T = c.T;
-    go.S = c.S;
-    go.G = grad;
-    go.scale = scale;
-    return launch_pass<N, AX_ROWS>(go, c.count, c.st, c.tw);
+    if constexpr (rowsio_ok<N>()) {
+      return launch_rows_io<N, ROWS_GRAD_OUT>(c, c.T, grad, scale);
+    } else {
+      OpRowsGradOut go;
+      go.first = c.first;
+      go.partials = nullptr;
+      go.T = c.T;
+      go.S = c.S;
+      go.G = grad;
+      go.scale = scale;
+      return launch_pass<N, AX_ROWS>(go, c.count, c.st, c.tw);
+    }
   }
   // loss (partials) at the current densities, then one Adam step in place
   template <int LOSS>
   static cudaError_t adam_step_t(const Ctx& c, float eps, double* partials, float2* m, float2* v, float b1, float b2,
                                  float step_size, float inv_sqrt_bc2, float adam_eps) {
-    OpRowsSupportForward rf;
-    rf.first = c.first;
-    rf.partials = nullptr;
-    rf.rho = c.rho;
-    rf.S = c.S;
-    rf.T = c.T;
-    SPE_TRY((launch_pass<N, AX_ROWS>(rf, c.count, c.st, c.tw)));
+    SPE_TRY(support_forward(c));
     constexpr int WL = DefaultTiles<N>::cols;
     SPE_TRY((launch_cols_loss<N, WL, LOSS, true>(c, eps, partials)));
     OpRowsGradAdam ad;
