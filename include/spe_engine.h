@@ -290,6 +290,20 @@ enum { SPE_LOSS_AMPLITUDE = 0, SPE_LOSS_POISSON = 1 };
 int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
                   double* loss_out, void* grad_out, const float* grad_scale);
 
+/* spe_loss_grad in two calls, for a backward pass that comes later (no
+ * reference counterpart).  spe_loss_grad_cols computes the loss into
+ * loss_out (may be NULL) and the adjoint up to its column pass, leaving the
+ * column-transformed gradient in `half` (device, complex64 count*n*n,
+ * caller-owned, not the density; it also holds the forward transform, so no
+ * engine scratch is used).  spe_grad_rows then runs the adjoint's last pass
+ * from `half` into grad_out times grad_scale (as in spe_loss_grad); grad_out
+ * may be `half` itself.  `half` must be left unchanged between the calls.
+ * The gradient equals spe_loss_grad's bit for bit. */
+int spe_loss_grad_cols(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
+                       double* loss_out, void* half);
+int spe_grad_rows(spe_engine* e, const void* half, const int32_t* support, int count, void* grad_out,
+                  const float* grad_scale);
+
 /* CUDA graphs of engine calls (no reference counterpart).  Between
  * spe_graph_begin(stream) and spe_graph_end(stream, &g), asynchronous engine
  * calls of one or more engines whose stream (spe_set_stream) is `stream` are

@@ -84,6 +84,8 @@ SIGNATURES = {
     "spe_iterate_host": (_i, [_vp, _i, _i, _fp, _ip, _i, _i, _f, _f, _fp, _i]),
     "spe_far_field": (_i, [_vp, _i, _i, _fp]),
     "spe_loss_grad": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp, _vp]),
+    "spe_loss_grad_cols": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp]),
+    "spe_grad_rows": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "spe_set_amplitudes_batch": (_i, [_vp, _fp, _i, _i]),
     "spe_adam_step": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _f, _f, _f, _f, _i, _vp]),
     "spe_get_rng_state": (_i, [_vp, C.c_char_p, _i, C.POINTER(_i)]),
@@ -389,6 +391,16 @@ class Engine:
         """Far-field loss / gradient on device arrays given by address."""
         call("spe_loss_grad", self.h, _vp(density_ptr), _vp(support_ptr), int(count), int(loss), float(eps),
              _vp(loss_ptr or 0), _vp(grad_ptr or 0), _vp(scale_ptr or 0))
+
+    def loss_grad_cols(self, density_ptr, support_ptr, count, half_ptr, loss=0, eps=0.0, loss_ptr=0):
+        """Loss and the adjoint up to its column pass, kept in ``half``."""
+        call("spe_loss_grad_cols", self.h, _vp(density_ptr), _vp(support_ptr), int(count), int(loss), float(eps),
+             _vp(loss_ptr or 0), _vp(half_ptr))
+
+    def grad_rows(self, half_ptr, support_ptr, count, grad_ptr, scale_ptr=0):
+        """The adjoint's last pass from ``half`` (grad may be half)."""
+        call("spe_grad_rows", self.h, _vp(half_ptr), _vp(support_ptr), int(count), _vp(grad_ptr),
+             _vp(scale_ptr or 0))
 
     def adam_step(self, density_ptr, support_ptr, m_ptr, v_ptr, count, loss=1, eps=0.0, lr=1e-3, beta1=0.9,
                   beta2=0.999, adam_eps=1e-8, step=1, loss_ptr=0):

@@ -870,29 +870,75 @@ int spe_set_tiles(spe_engine* e, int cols, int rows) {
   return SPE_OK;
 }
 
+// checks shared by the loss entry points; 1 when there is nothing to do
+static int loss_args(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
+                     int* rc) {
+  *rc = SPE_OK;
+  if (!e) return (*rc = fail(SPE_ERR_INVALID, "null engine")), 1;
+  if ((*rc = need_amp(e))) return 1;
+  if (count < 0) return (*rc = fail(SPE_ERR_INVALID, "negative count")), 1;
+  if (loss != SPE_LOSS_AMPLITUDE && loss != SPE_LOSS_POISSON)
+    return (*rc = fail(SPE_ERR_INVALID, "unknown loss %d", loss)), 1;
+  if (!(eps >= 0.f)) return (*rc = fail(SPE_ERR_INVALID, "eps must be >= 0")), 1;
+  if (count == 0) return 1;
+  if (!density || !support) return (*rc = fail(SPE_ERR_INVALID, "null density or support")), 1;
+  return 0;
+}
+
+// per-item losses from the column-pass partials into loss_out
+static int loss_sums(spe_engine* e, int count, double* loss_out) {
+  int rc = reduce(e, e->partials, count, e->ops->loss_tiles, 0, 0, 0);
+  if (rc) return rc;
+  CK(cudaMemcpy2DAsync(loss_out, sizeof(double), e->red, 16 * sizeof(double), sizeof(double), count,
+                       cudaMemcpyDeviceToDevice, e->st),
+     "loss copy");
+  return SPE_OK;
+}
+
 int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
                   double* loss_out, void* grad_out, const float* grad_scale) {
-  if (!e) return fail(SPE_ERR_INVALID, "null engine");
-  int rc = need_amp(e);
-  if (rc) return rc;
-  if (count < 0) return fail(SPE_ERR_INVALID, "negative count");
-  if (loss != SPE_LOSS_AMPLITUDE && loss != SPE_LOSS_POISSON) return fail(SPE_ERR_INVALID, "unknown loss %d", loss);
-  if (!(eps >= 0.f)) return fail(SPE_ERR_INVALID, "eps must be >= 0");
-  if (count == 0) return SPE_OK;
-  if (!density || !support) return fail(SPE_ERR_INVALID, "null density or support");
+  int rc;
+  if (loss_args(e, density, support, count, loss, eps, &rc)) return rc;
   if (!loss_out && !grad_out) return SPE_OK;
   if ((rc = spe_reserve(e, count))) return rc;  // scratch and partials for `count` items
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   spe::Ctx c = make_ctx(e, 0, count);
   c.rho = static_cast<float2*>(const_cast<void*>(density));
   c.S = const_cast<int*>(support);
-  CK(e->ops->loss_grad(c, loss, eps, e->partials, static_cast<float2*>(grad_out), grad_scale), "loss kernels");
-  if (loss_out) {
-    if ((rc = reduce(e, e->partials, count, e->ops->loss_tiles, 0, 0, 0))) return rc;
-    CK(cudaMemcpy2DAsync(loss_out, sizeof(double), e->red, 16 * sizeof(double), sizeof(double), count,
-                         cudaMemcpyDeviceToDevice, e->st),
-       "loss copy");
-  }
+  CK(e->ops->loss_grad(c, loss, eps, e->partials, static_cast<float2*>(grad_out), grad_scale, spe::GRAD_ALL),
+     "loss kernels");
+  return loss_out ? loss_sums(e, count, loss_out) : SPE_OK;
+}
+
+int spe_loss_grad_cols(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
+                       double* loss_out, void* half) {
+  int rc;
+  if (loss_args(e, density, support, count, loss, eps, &rc)) return rc;
+  if (!half) return fail(SPE_ERR_INVALID, "null gradient buffer");
+  if (half == density) return fail(SPE_ERR_INVALID, "the gradient buffer must not be the density");
+  if ((rc = spe_reserve(e, count))) return rc;  // partials for `count` items
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  spe::Ctx c = make_ctx(e, 0, count);
+  c.rho = static_cast<float2*>(const_cast<void*>(density));
+  c.S = const_cast<int*>(support);
+  c.T = static_cast<float2*>(half);  // the forward transform and the adjoint's column pass run in `half`
+  CK(e->ops->loss_grad(c, loss, eps, e->partials, c.T, nullptr, spe::GRAD_COLS), "loss kernels");
+  return loss_out ? loss_sums(e, count, loss_out) : SPE_OK;
+}
+
+int spe_grad_rows(spe_engine* e, const void* half, const int32_t* support, int count, void* grad_out,
+                  const float* grad_scale) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  if (count < 0) return fail(SPE_ERR_INVALID, "negative count");
+  if (count == 0) return SPE_OK;
+  if (!half || !support || !grad_out) return fail(SPE_ERR_INVALID, "null gradient buffer, support or output");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  spe::Ctx c = make_ctx(e, 0, count);
+  c.S = const_cast<int*>(support);
+  c.T = static_cast<float2*>(const_cast<void*>(half));
+  CK(e->ops->loss_grad(c, SPE_LOSS_AMPLITUDE, 0.f, nullptr, static_cast<float2*>(grad_out), grad_scale,
+                       spe::GRAD_ROWS),
+     "gradient row pass");
   return SPE_OK;
 }
 

@@ -9,6 +9,9 @@
 
 namespace spe {
 
+// Stages of the far-field loss gradient (SizeOps::loss_grad).
+enum { GRAD_ALL = 0, GRAD_COLS = 1, GRAD_ROWS = 2 };
+
 // Host pattern encoding (spe_host.cpp).
 int prepare_pattern(const float* in, int n, int cx, int cy, bool use_bounds, float* out);
 
@@ -118,8 +121,12 @@ struct SizeOps {
   cudaError_t (*known_power)(const Ctx&, double* partials);
   // far-field loss (0 amplitude, 1 Poisson) of items [first, first+count) of
   // Ctx::rho / Ctx::S into column-pass partials; with grad, the adjoint
-  // gradient times scale[item] (scale may be null)
-  cudaError_t (*loss_grad)(const Ctx&, int loss, float eps, double* partials, float2* grad, const float* scale);
+  // gradient times scale[item] (scale may be null).  stage GRAD_COLS stops
+  // after the column pass (the column-transformed gradient left in Ctx::T);
+  // GRAD_ROWS runs only the last pass, from Ctx::T into grad (which may be
+  // Ctx::T: every row is read whole before it is written)
+  cudaError_t (*loss_grad)(const Ctx&, int loss, float eps, double* partials, float2* grad, const float* scale,
+                           int stage);
   int loss_tiles;  // loss partials per item
   // loss at the current densities into partials, then one Adam step in
   // place with moments m, v (see OpRowsGradAdam)

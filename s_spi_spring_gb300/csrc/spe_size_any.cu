@@ -557,9 +557,21 @@ struct SizeAny {
   }
 
   // far-field loss: one partial per column tile (loss_tiles = tiles_cols)
+  static cudaError_t grad_rows(const Ctx& c, const AnyPlan& pl, float2* grad, const float* scale) {
+    OpRowsGradOut go;
+    go.first = c.first;
+    go.partials = nullptr;
+    go.T = c.T;
+    go.S = c.S;
+    go.G = grad;
+    go.scale = scale;
+    return launch_any<AX_ROWS>(go, pl, c.count, c.st, c.tw);
+  }
   template <int LOSS>
-  static cudaError_t loss_grad_t(const Ctx& c, float eps, double* partials, float2* grad, const float* scale) {
+  static cudaError_t loss_grad_t(const Ctx& c, float eps, double* partials, float2* grad, const float* scale,
+                                 int stage) {
     const AnyPlan& pl = plan_of(c.n);
+    if (stage == GRAD_ROWS) return grad_rows(c, pl, grad, scale);
     OpRowsSupportForward rf;
     rf.first = c.first;
     rf.partials = nullptr;
@@ -567,7 +579,7 @@ struct SizeAny {
     rf.S = c.S;
     rf.T = c.T;
     SPE_TRY((launch_any<AX_ROWS>(rf, pl, c.count, c.st, c.tw)));
-    if (!grad) {
+    if (!grad && stage == GRAD_ALL) {
       OpColsLoss<LOSS, false> cl;
       cl.first = c.first;
       cl.partials = partials;
@@ -587,20 +599,14 @@ struct SizeAny {
     cl.ipp = c.ipp;
     cl.eps = eps;
     SPE_TRY((launch_any<AX_COLS>(cl, pl, c.count, c.st, c.tw)));
-    OpRowsGradOut go;
-    go.first = c.first;
-    go.partials = nullptr;
-    go.T = c.T;
-    go.S = c.S;
-    go.G = grad;
-    go.scale = scale;
-    return launch_any<AX_ROWS>(go, pl, c.count, c.st, c.tw);
+    if (stage == GRAD_COLS) return cudaSuccess;
+    return grad_rows(c, pl, grad, scale);
   }
 
   static cudaError_t loss_grad(const Ctx& c, int loss, float eps, double* partials, float2* grad,
-                               const float* scale) {
-    return loss == LOSS_POISSON ? loss_grad_t<LOSS_POISSON>(c, eps, partials, grad, scale)
-                                : loss_grad_t<LOSS_AMPLITUDE>(c, eps, partials, grad, scale);
+                               const float* scale, int stage) {
+    return loss == LOSS_POISSON ? loss_grad_t<LOSS_POISSON>(c, eps, partials, grad, scale, stage)
+                                : loss_grad_t<LOSS_AMPLITUDE>(c, eps, partials, grad, scale, stage);
   }
 
   template <int LOSS>

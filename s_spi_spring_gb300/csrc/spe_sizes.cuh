@@ -733,12 +733,8 @@ struct SizeImpl {
     }
   }
 
-  template <int LOSS>
-  static cudaError_t loss_grad_t(const Ctx& c, float eps, double* partials, float2* grad, const float* scale) {
-    SPE_TRY(support_forward(c));
-    constexpr int WL = DefaultTiles<N>::cols;  // loss partials: N / WL per item
-    if (!grad) return launch_cols_loss<N, WL, LOSS, false>(c, eps, partials);
-    SPE_TRY((launch_cols_loss<N, WL, LOSS, true>(c, eps, partials)));
+  // the last pass of the adjoint: T -> FFT- (x) -> grad = scale[p] * S * .
+  static cudaError_t grad_rows(const Ctx& c, float2* grad, const float* scale) {
     if constexpr (rowsio_ok<N>()) {
       return launch_rows_io<N, ROWS_GRAD_OUT>(c, c.T, grad, scale);
     } else {
@@ -751,6 +747,17 @@ struct SizeImpl {
       go.scale = scale;
       return launch_pass<N, AX_ROWS>(go, c.count, c.st, c.tw);
     }
+  }
+  template <int LOSS>
+  static cudaError_t loss_grad_t(const Ctx& c, float eps, double* partials, float2* grad, const float* scale,
+                                 int stage) {
+    if (stage == GRAD_ROWS) return grad_rows(c, grad, scale);
+    SPE_TRY(support_forward(c));
+    constexpr int WL = DefaultTiles<N>::cols;  // loss partials: N / WL per item
+    if (!grad && stage == GRAD_ALL) return launch_cols_loss<N, WL, LOSS, false>(c, eps, partials);
+    SPE_TRY((launch_cols_loss<N, WL, LOSS, true>(c, eps, partials)));
+    if (stage == GRAD_COLS) return cudaSuccess;
+    return grad_rows(c, grad, scale);
   }
   // loss (partials) at the current densities, then one Adam step in place
   template <int LOSS>
@@ -782,9 +789,9 @@ struct SizeImpl {
   }
 
   static cudaError_t loss_grad(const Ctx& c, int loss, float eps, double* partials, float2* grad,
-                               const float* scale) {
-    return loss == LOSS_POISSON ? loss_grad_t<LOSS_POISSON>(c, eps, partials, grad, scale)
-                                : loss_grad_t<LOSS_AMPLITUDE>(c, eps, partials, grad, scale);
+                               const float* scale, int stage) {
+    return loss == LOSS_POISSON ? loss_grad_t<LOSS_POISSON>(c, eps, partials, grad, scale, stage)
+                                : loss_grad_t<LOSS_AMPLITUDE>(c, eps, partials, grad, scale, stage);
   }
 
   static const SizeOps* table() {

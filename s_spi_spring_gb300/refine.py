@@ -2,9 +2,11 @@
 
 ``FarFieldLoss`` is a ``torch.autograd.Function`` over the engine's
 hand-written loss and adjoint kernels (``spe_loss_grad``): the forward pass
-returns the per-individual loss of the masked far field, the backward pass
-recomputes the transform (no intermediate is stored between the two) and
-applies the adjoint through FFT, mask and support.  Bulk arithmetic is FP32;
+returns the per-individual loss of the masked far field and, up to a size
+bound, keeps the adjoint's column-transformed gradient, so that the backward
+pass is one row pass (FFT, support, upstream scale); above the bound the
+backward pass recomputes the transform and the whole adjoint.  Bulk
+arithmetic is FP32;
 the per-individual loss sums are FP64.
 
 ``refine`` runs Adam on individuals that stay in the engine's population
@@ -65,14 +67,13 @@ class FarFieldLoss(torch.autograd.Function):
     to `density` only (complex autograd convention).
 
     With a gradient of at most STORE_GRADIENT_BYTES (or recompute=False) the
-    forward pass computes the loss and the unscaled gradient in one set of
-    passes (rows, columns with the adjoint, rows out) and keeps the gradient;
-    the backward pass only multiplies it by the upstream gradient (one
-    elementwise pass).  Above that size (or with
-    recompute=True) nothing is kept: the backward pass recomputes the
-    transform and applies the adjoint with the upstream scale fused in.  Both
-    give bit-identical gradients (the fused scale multiplies the same values
-    the stored path multiplies, and a scale of 1 is exact)."""
+    forward pass computes the loss and the adjoint up to its column pass in
+    one set of passes (``spe_loss_grad_cols``) and keeps that half-transformed
+    gradient; the backward pass is the adjoint's last row pass with the
+    upstream scale fused in, in place (``spe_grad_rows``).  Above that size
+    (or with recompute=True) nothing is kept: the backward pass recomputes the
+    transform and the whole adjoint (``spe_loss_grad``).  Both run the same
+    kernels on the same values, so the gradients are bit-identical."""
 
     @staticmethod
     def forward(ctx, density, support, engine, loss="amplitude", eps=0.0, recompute=None):
@@ -85,14 +86,14 @@ class FarFieldLoss(torch.autograd.Function):
         out = torch.empty(count, dtype=torch.float64, device=density.device)
         if recompute is None:
             recompute = density.numel() * density.element_size() > STORE_GRADIENT_BYTES
-        ctx.grad = None
+        ctx.half = None
         if recompute or not ctx.needs_input_grad[0]:
             engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[loss], eps, out.data_ptr(), 0, 0)
         else:
-            grad = torch.empty_like(density)
-            engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[loss], eps, out.data_ptr(),
-                             grad.data_ptr(), 0)
-            ctx.grad = grad
+            half = torch.empty_like(density)
+            engine.loss_grad_cols(density.data_ptr(), support.data_ptr(), count, half.data_ptr(), LOSSES[loss], eps,
+                                  out.data_ptr())
+            ctx.half = half
         ctx.save_for_backward(density, support)
         ctx.engine, ctx.loss, ctx.eps = engine, loss, eps
         return out
@@ -102,16 +103,12 @@ class FarFieldLoss(torch.autograd.Function):
         density, support = ctx.saved_tensors
         count = density.shape[0]
         scale = grad_out.to(torch.float32).contiguous()
-        if ctx.grad is not None:
-            grad, ctx.grad = ctx.grad, None
-            # real and imaginary parts scaled separately, in place, as the
-            # kernel does (a complex-by-real product in torch would add +-0
-            # terms and turn -0 into +0); no host check of the scale, which
-            # would wait for the device
-            torch.view_as_real(grad).mul_(scale.view(-1, *([1] * grad.dim())))
+        _bind_stream(ctx.engine, density.device)
+        if ctx.half is not None:
+            grad, ctx.half = ctx.half, None
+            ctx.engine.grad_rows(grad.data_ptr(), support.data_ptr(), count, grad.data_ptr(), scale.data_ptr())
             return grad, None, None, None, None, None
         grad = torch.empty_like(density)
-        _bind_stream(ctx.engine, density.device)
         ctx.engine.loss_grad(density.data_ptr(), support.data_ptr(), count, LOSSES[ctx.loss], ctx.eps, 0,
                              grad.data_ptr(), scale.data_ptr())
         return grad, None, None, None, None, None

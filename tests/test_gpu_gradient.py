@@ -128,13 +128,17 @@ def test_fused_adam_matches_autograd_adam(loss):
     assert ha[-1] < ha[0]
 
 
+@pytest.mark.parametrize("n", [100, 128, 512, 2048])
 @pytest.mark.parametrize("loss,eps", [("amplitude", 0.0), ("poisson", 1e-3)])
-def test_stored_and_recomputed_gradients_are_bit_identical(loss, eps):
-    """FarFieldLoss computes the gradient with the loss and keeps it (small
-    sizes), or recomputes it in the backward pass with the upstream scale
-    fused (large sizes): the same bits either way, with unit and non-unit
-    upstream gradients."""
-    n, P = 128, 3
+def test_stored_and_recomputed_gradients_are_bit_identical(n, loss, eps):
+    """FarFieldLoss keeps the adjoint's column-transformed gradient from the
+    forward pass and finishes it in place in the backward pass
+    (spe_loss_grad_cols, spe_grad_rows; small sizes), or recomputes the whole
+    adjoint there (spe_loss_grad; large sizes): the same bits either way,
+    with unit and non-unit upstream gradients, on a side without a compiled
+    plan (100), the generic row pass (128, 2048) and the staged row pass
+    (512)."""
+    P = 3
     eng, A, dens, S = setup(n, P, seed=21)
     s = torch.tensor(S, device=DEV)
     for weights in (None, np.array([1.0, 0.5, 2.0])):
@@ -147,3 +151,35 @@ def test_stored_and_recomputed_gradients_are_bit_identical(loss, eps):
             out.append((L.detach().cpu().numpy(), d.grad.cpu().numpy()))
         assert np.array_equal(out[0][0], out[1][0])
         assert np.array_equal(out[0][1].view(np.uint32), out[1][1].view(np.uint32))
+
+
+def test_split_gradient_out_of_place_and_argument_checks():
+    """spe_grad_rows into a separate buffer gives the in-place result and
+    spe_loss_grad's; the entry points refuse a null buffer and a buffer that
+    is the density."""
+    n, P = 256, 2
+    eng, A, dens, S = setup(n, P, seed=5)
+    d = torch.tensor(dens, device=DEV)
+    s = torch.tensor(S, device=DEV)
+    scale = torch.tensor([0.75, 3.0], device=DEV)
+    half = torch.empty_like(d)
+    loss = torch.empty(P, dtype=torch.float64, device=DEV)
+    eng.set_stream(torch.cuda.current_stream(DEV).cuda_stream or 1)
+    eng.loss_grad_cols(d.data_ptr(), s.data_ptr(), P, half.data_ptr(), 1, 1e-3, loss.data_ptr())
+    out = torch.empty_like(d)
+    eng.grad_rows(half.data_ptr(), s.data_ptr(), P, out.data_ptr(), scale.data_ptr())
+    eng.grad_rows(half.data_ptr(), s.data_ptr(), P, half.data_ptr(), scale.data_ptr())
+    full = torch.empty_like(d)
+    loss2 = torch.empty(P, dtype=torch.float64, device=DEV)
+    eng.loss_grad(d.data_ptr(), s.data_ptr(), P, 1, 1e-3, loss2.data_ptr(), full.data_ptr(), scale.data_ptr())
+    torch.cuda.synchronize(DEV)
+    assert torch.equal(loss, loss2)
+    assert torch.equal(torch.view_as_real(out).view(torch.int32), torch.view_as_real(full).view(torch.int32))
+    assert torch.equal(torch.view_as_real(half).view(torch.int32), torch.view_as_real(full).view(torch.int32))
+    with pytest.raises(RuntimeError):
+        eng.loss_grad_cols(d.data_ptr(), s.data_ptr(), P, 0, 1, 1e-3, 0)
+    with pytest.raises(RuntimeError):
+        eng.loss_grad_cols(d.data_ptr(), s.data_ptr(), P, d.data_ptr(), 1, 1e-3, 0)
+    with pytest.raises(RuntimeError):
+        eng.grad_rows(half.data_ptr(), s.data_ptr(), P, 0)
+    eng.close()
