@@ -285,7 +285,10 @@ int spe_get_tiles(spe_engine* e, int* cols, int* rows);
  * complex autograd.  The transform is recomputed, nothing is stored between
  * the loss and the gradient.  Runs on the engine's stream; the engine's
  * population capacity grows to `count` for scratch, so arrays that alias the
- * engine's own slots (spe_device_buffers) need count <= spe_capacity. */
+ * engine's own slots (spe_device_buffers) need count <= spe_capacity.
+ * density and support must start on a 16-byte boundary (the kernels stage
+ * them with 16-byte copies; cudaMalloc'd arrays do), else SPE_ERR_INVALID
+ * (sides with a compiled plan; the other sides take any address). */
 enum { SPE_LOSS_AMPLITUDE = 0, SPE_LOSS_POISSON = 1 };
 int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
                   double* loss_out, void* grad_out, const float* grad_scale);
@@ -298,7 +301,8 @@ int spe_loss_grad(spe_engine* e, const void* density, const int32_t* support, in
  * engine scratch is used).  spe_grad_rows then runs the adjoint's last pass
  * from `half` into grad_out times grad_scale (as in spe_loss_grad); grad_out
  * may be `half` itself.  `half` must be left unchanged between the calls.
- * The gradient equals spe_loss_grad's bit for bit. */
+ * The gradient equals spe_loss_grad's bit for bit.  density, support and
+ * half must start on a 16-byte boundary. */
 int spe_loss_grad_cols(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
                        double* loss_out, void* half);
 int spe_grad_rows(spe_engine* e, const void* half, const int32_t* support, int count, void* grad_out,
@@ -332,7 +336,8 @@ int spe_graph_destroy(spe_graph* g);
  * in exp_avg / exp_avg_sq (device, complex64 layout, count*n*n each, zero
  * before step 1).  `step` counts from 1.  The gradient never reaches memory:
  * the last pass of the adjoint applies the update.  As for spe_loss_grad,
- * arrays aliasing the engine's slots need count <= spe_capacity. */
+ * arrays aliasing the engine's slots need count <= spe_capacity, and every
+ * device array must start on a 16-byte boundary. */
 int spe_adam_step(spe_engine* e, void* density, const int32_t* support, void* exp_avg, void* exp_avg_sq, int count,
                   int loss, float eps, float lr, float beta1, float beta2, float adam_eps, int step,
                   double* loss_out);
@@ -416,7 +421,9 @@ int spe_device_info(int device, char* name, int name_len, char* pci_bus_id, int 
  * device.  Same arithmetic as spe_hio / spe_raar / spe_er, but on device
  * arrays the caller owns: density (count*n*n complex64, updated in place),
  * support (count*n*n int32), amplitudes (n*n float, the output of
- * spe_prepare_pattern); algorithm is SPE_OP_HIO, SPE_OP_RAAR or SPE_OP_ER;
+ * spe_prepare_pattern), each starting on a 16-byte boundary (as cudaMalloc'd
+ * arrays do; others are rejected with SPE_ERR_INVALID); algorithm is
+ * SPE_OP_HIO, SPE_OP_RAAR or SPE_OP_ER;
  * work is queued on cuda_stream (a cudaStream_t of the current device,
  * NULL: the legacy stream; a stream of another device is rejected with
  * SPE_ERR_INVALID).  The scratch lives in a 16 MiB file-scope device array

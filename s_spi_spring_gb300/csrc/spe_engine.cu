@@ -870,6 +870,14 @@ int spe_set_tiles(spe_engine* e, int cols, int rows) {
   return SPE_OK;
 }
 
+// Device arrays that the persistent kernels of the compiled sides stage
+// with 16-byte cp.async copies must start on a 16-byte boundary (cudaMalloc
+// and torch allocations do; a view at an odd complex64 offset does not).
+// The run-time kernels of the other sides (default_cols 0) load plainly.
+static bool misaligned16(const spe_engine* e, const void* p) {
+  return e->ops->default_cols > 0 && (reinterpret_cast<uintptr_t>(p) & 15u) != 0;
+}
+
 // checks shared by the loss entry points; 1 when there is nothing to do
 static int loss_args(spe_engine* e, const void* density, const int32_t* support, int count, int loss, float eps,
                      int* rc) {
@@ -882,6 +890,8 @@ static int loss_args(spe_engine* e, const void* density, const int32_t* support,
   if (!(eps >= 0.f)) return (*rc = fail(SPE_ERR_INVALID, "eps must be >= 0")), 1;
   if (count == 0) return 1;
   if (!density || !support) return (*rc = fail(SPE_ERR_INVALID, "null density or support")), 1;
+  if (misaligned16(e, density) || misaligned16(e, support))
+    return (*rc = fail(SPE_ERR_INVALID, "density and support must start on a 16-byte boundary")), 1;
   return 0;
 }
 
@@ -915,6 +925,7 @@ int spe_loss_grad_cols(spe_engine* e, const void* density, const int32_t* suppor
   int rc;
   if (loss_args(e, density, support, count, loss, eps, &rc)) return rc;
   if (!half) return fail(SPE_ERR_INVALID, "null gradient buffer");
+  if (misaligned16(e, half)) return fail(SPE_ERR_INVALID, "the gradient buffer must start on a 16-byte boundary");
   if (half == density) return fail(SPE_ERR_INVALID, "the gradient buffer must not be the density");
   if ((rc = spe_reserve(e, count))) return rc;  // partials for `count` items
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
@@ -932,6 +943,8 @@ int spe_grad_rows(spe_engine* e, const void* half, const int32_t* support, int c
   if (count < 0) return fail(SPE_ERR_INVALID, "negative count");
   if (count == 0) return SPE_OK;
   if (!half || !support || !grad_out) return fail(SPE_ERR_INVALID, "null gradient buffer, support or output");
+  if (misaligned16(e, half) || misaligned16(e, support))
+    return fail(SPE_ERR_INVALID, "the gradient buffer and the support must start on a 16-byte boundary");
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   spe::Ctx c = make_ctx(e, 0, count);
   c.S = const_cast<int*>(support);
@@ -1014,6 +1027,8 @@ int spe_adam_step(spe_engine* e, void* density, const int32_t* support, void* ex
     return fail(SPE_ERR_INVALID, "invalid optimiser parameters");
   if (count == 0) return SPE_OK;
   if (!density || !support || !exp_avg || !exp_avg_sq) return fail(SPE_ERR_INVALID, "null device array");
+  if (misaligned16(e, density) || misaligned16(e, support) || misaligned16(e, exp_avg) || misaligned16(e, exp_avg_sq))
+    return fail(SPE_ERR_INVALID, "density, support and moments must start on a 16-byte boundary");
   if ((rc = spe_reserve(e, count))) return rc;
   CK(cudaSetDevice(e->dev), "cudaSetDevice");
   // torch.optim.Adam's bias corrections, in double

@@ -116,7 +116,7 @@ struct SizeOps {
   // tile widths compiled for this size
   int (*col_widths)(int* out);
   int (*row_widths)(int* out);
-  int default_cols, default_rows;
+  int default_cols, default_rows;  // 0 for sides without a compiled plan
   // partials of the column pass: sum over A >= 0 of |FFT+(rho)|^2 and A^2
   cudaError_t (*known_power)(const Ctx&, double* partials);
   // far-field loss (0 amplitude, 1 Poisson) of items [first, first+count) of

@@ -715,6 +715,23 @@ struct OpRowsGradOut : OpBase {
 //   rho -= step_size * m / (sqrt(v) / sqrt_bc2 + eps)
 // (step_size = lr / (1 - b1^t), sqrt_bc2 = sqrt(1 - b2^t): torch.optim.Adam
 // without weight decay, complex parameters as pairs of reals)
+struct AdamParams {
+  float b1, b2, step_size, inv_sqrt_bc2, eps;
+  // one real component: moments mm, vv and parameter p after gradient g
+  __device__ __forceinline__ float upd(float g, float& mm, float& vv, float p) const {
+    mm = mm + (1.f - b1) * (g - mm);
+    vv = vv * b2 + (1.f - b2) * g * g;
+    const float den = sqrtf(vv) * inv_sqrt_bc2 + eps;
+    return p - step_size * (mm / den);
+  }
+  // a complex pixel: gradient g (zeroed outside the support s)
+  __device__ __forceinline__ void step(float2 g, int s, float2& mm, float2& vv, float2& p) const {
+    if (s <= 0) g = make_float2(0.f, 0.f);
+    p.x = upd(g.x, mm.x, vv.x, p.x);
+    p.y = upd(g.y, mm.y, vv.y, p.y);
+  }
+};
+
 struct OpRowsGradAdam : OpBase {
   static constexpr int FFT1 = -1, FFT2 = 0, NSUM = 0, NMAX = 0;
   const float2* T;
@@ -722,21 +739,13 @@ struct OpRowsGradAdam : OpBase {
   float2* rho;
   float2* m;
   float2* v;
-  float b1, b2, step_size, inv_sqrt_bc2, eps;
+  AdamParams ap;
   using Acc = NoAcc;
   __device__ float2 load(size_t gi, int, int, int, Acc&) const { return T[gi]; }
   __device__ float2 mid(float2 x, size_t, int, int, int, Acc&) const { return x; }
-  __device__ __forceinline__ float upd(float g, float& mm, float& vv, float p) const {
-    mm = mm + (1.f - b1) * (g - mm);
-    vv = vv * b2 + (1.f - b2) * g * g;
-    const float den = sqrtf(vv) * inv_sqrt_bc2 + eps;
-    return p - step_size * (mm / den);
-  }
   __device__ void store(float2 g, size_t gi, int, int, int, Acc&) const {
-    if (S[gi] <= 0) g = make_float2(0.f, 0.f);
     float2 mm = m[gi], vv = v[gi], p = rho[gi];
-    p.x = upd(g.x, mm.x, vv.x, p.x);
-    p.y = upd(g.y, mm.y, vv.y, p.y);
+    ap.step(g, S[gi], mm, vv, p);
     m[gi] = mm;
     v[gi] = vv;
     rho[gi] = p;

@@ -91,6 +91,10 @@ extern "C" int spe_iterate_noalloc(int n, void* density, const int32_t* support,
   const spe::SizeOps* ops = spe::size_ops(n);
   if (!ops) return fail(SPE_ERR_UNSUPPORTED, "pattern side %d has no compiled FFT plan", n);
   if (!density || !support || !amplitudes) return fail(SPE_ERR_INVALID, "null device array");
+  // the kernels stage their rows and columns with 16-byte cp.async copies
+  if (((reinterpret_cast<uintptr_t>(density) | reinterpret_cast<uintptr_t>(support) |
+        reinterpret_cast<uintptr_t>(amplitudes)) & 15u) != 0)
+    return fail(SPE_ERR_INVALID, "density, support and amplitudes must start on a 16-byte boundary");
   if (count < 0 || iterations < 0) return fail(SPE_ERR_INVALID, "negative count or iteration number");
   if (algorithm != SPE_OP_HIO && algorithm != SPE_OP_RAAR && algorithm != SPE_OP_ER)
     return fail(SPE_ERR_INVALID, "algorithm must be SPE_OP_HIO, SPE_OP_RAAR or SPE_OP_ER");

@@ -637,11 +637,7 @@ struct SizeAny {
     ad.rho = c.rho;
     ad.m = m;
     ad.v = v;
-    ad.b1 = b1;
-    ad.b2 = b2;
-    ad.step_size = step_size;
-    ad.inv_sqrt_bc2 = inv_sqrt_bc2;
-    ad.eps = adam_eps;
+    ad.ap = {b1, b2, step_size, inv_sqrt_bc2, adam_eps};
     return launch_any<AX_ROWS>(ad, pl, c.count, c.st, c.tw);
   }
 

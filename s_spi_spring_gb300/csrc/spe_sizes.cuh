@@ -774,11 +774,7 @@ struct SizeImpl {
     ad.rho = c.rho;
     ad.m = m;
     ad.v = v;
-    ad.b1 = b1;
-    ad.b2 = b2;
-    ad.step_size = step_size;
-    ad.inv_sqrt_bc2 = inv_sqrt_bc2;
-    ad.eps = adam_eps;
+    ad.ap = {b1, b2, step_size, inv_sqrt_bc2, adam_eps};
     return launch_pass<N, AX_ROWS>(ad, c.count, c.st, c.tw);
   }
   static cudaError_t adam_step(const Ctx& c, int loss, float eps, double* partials, float2* m, float2* v, float b1,

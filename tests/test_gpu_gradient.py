@@ -108,12 +108,14 @@ def test_refine_in_place_on_population_slots():
           [round(m["error_fourier"], 4) for m in m1])
 
 
+@pytest.mark.parametrize("n", [100, 128, 256, 512, 1024])
 @pytest.mark.parametrize("loss", ["amplitude", "poisson"])
-def test_fused_adam_matches_autograd_adam(loss):
+def test_fused_adam_matches_autograd_adam(n, loss):
     """The fused refinement step (loss, adjoint and Adam update on the
     device) against FarFieldLoss + torch.optim.Adam: the same loss history
-    and densities within FP32 rounding."""
-    n, P = 128, 3
+    and densities within FP32 rounding, at compiled sides (staged loss row
+    passes from 256) and at a side without a compiled plan (100)."""
+    P = 3
     eng_a, A, dens, S = setup(n, P, seed=12)
     eng_b, _, _, _ = setup(n, P, seed=12)
     for e in (eng_a, eng_b):
@@ -182,4 +184,52 @@ def test_split_gradient_out_of_place_and_argument_checks():
         eng.loss_grad_cols(d.data_ptr(), s.data_ptr(), P, d.data_ptr(), 1, 1e-3, 0)
     with pytest.raises(RuntimeError):
         eng.grad_rows(half.data_ptr(), s.data_ptr(), P, 0)
+    eng.close()
+
+
+def test_misaligned_device_arrays_are_refused():
+    """The compiled sides stage caller arrays with 16-byte copies: arrays
+    that do not start on a 16-byte boundary (here a view one complex64
+    element in) are refused on the host before any launch, and the engine
+    stays usable; a side without a compiled plan takes them."""
+    n, P = 256, 2
+    eng, A, dens, S = setup(n, P, seed=6)
+    eng.set_stream(torch.cuda.current_stream(DEV).cuda_stream or 1)
+    d = torch.tensor(dens, device=DEV)
+    s = torch.tensor(S, device=DEV)
+    raw = torch.zeros(P * n * n + 1, dtype=torch.complex64, device=DEV)
+    odd = raw[1:]  # 8 bytes past a 256-byte boundary
+    assert odd.data_ptr() % 16 == 8
+    odd_s = torch.zeros(P * n * n + 1, dtype=torch.int32, device=DEV)[1:]
+    good = torch.zeros_like(d)
+    with pytest.raises(RuntimeError, match="16-byte"):
+        eng.loss_grad(odd.data_ptr(), s.data_ptr(), P, 1, 1e-3, 0, good.data_ptr(), 0)
+    with pytest.raises(RuntimeError, match="16-byte"):
+        eng.loss_grad(d.data_ptr(), odd_s.data_ptr(), P, 1, 1e-3, 0, good.data_ptr(), 0)
+    with pytest.raises(RuntimeError, match="16-byte"):
+        eng.loss_grad_cols(d.data_ptr(), s.data_ptr(), P, odd.data_ptr(), 1, 1e-3, 0)
+    with pytest.raises(RuntimeError, match="16-byte"):
+        eng.grad_rows(odd.data_ptr(), s.data_ptr(), P, good.data_ptr())
+    with pytest.raises(RuntimeError, match="16-byte"):
+        eng.adam_step(d.data_ptr(), s.data_ptr(), odd.data_ptr(), good.data_ptr(), P)
+    # the engine is unaffected
+    loss = torch.empty(P, dtype=torch.float64, device=DEV)
+    eng.loss_grad(d.data_ptr(), s.data_ptr(), P, 1, 1e-3, loss.data_ptr(), good.data_ptr(), 0)
+    torch.cuda.synchronize(DEV)
+    assert torch.isfinite(loss).all()
+    eng.close()
+    # side 100 (run-time kernels, plain loads): the same views are accepted
+    n = 100
+    eng, A, dens, S = setup(n, 1, seed=6)
+    eng.set_stream(torch.cuda.current_stream(DEV).cuda_stream or 1)
+    raw = torch.zeros(n * n + 1, dtype=torch.complex64, device=DEV)
+    raw[1:] = torch.tensor(dens[0].ravel(), device=DEV)
+    s = torch.tensor(S[0], device=DEV)
+    loss_odd = torch.empty(1, dtype=torch.float64, device=DEV)
+    loss_ref = torch.empty(1, dtype=torch.float64, device=DEV)
+    eng.loss_grad(raw[1:].data_ptr(), s.data_ptr(), 1, 1, 1e-3, loss_odd.data_ptr(), 0, 0)
+    d = torch.tensor(dens[:1], device=DEV)
+    eng.loss_grad(d.data_ptr(), s.data_ptr(), 1, 1, 1e-3, loss_ref.data_ptr(), 0, 0)
+    torch.cuda.synchronize(DEV)
+    assert torch.equal(loss_odd, loss_ref)
     eng.close()

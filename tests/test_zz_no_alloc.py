@@ -10,7 +10,8 @@ one left): it launches the same kernels with the same tiles, so the results
 must be bit-identical.  The first call runs on a non-blocking stream (which
 the legacy-stream twiddle upload of the set-up does not order by itself);
 a repeated call must leave the device's free memory and torch's allocation
-unchanged; populations too large for the array are rejected.  This file
+unchanged; populations too large for the array, and arrays off a 16-byte
+boundary, are rejected.  This file
 sorts last so that a failure here comes after every other test.
 """
 import ctypes as C
@@ -119,3 +120,20 @@ def test_noalloc_rejects_populations_beyond_its_scratch():
     with pytest.raises(_lib.EngineError) as ei:
         _noalloc(torch, n, A, dens, S, _lib.SPE_OP_ER, 1, 0.0, 0.0)
     assert ei.value.code == 1 and "scratch" in str(ei.value)
+
+
+def test_noalloc_rejects_arrays_off_a_16_byte_boundary():
+    """The kernels stage rows and columns with 16-byte copies: a density
+    view one complex64 element into its allocation is refused on the host,
+    before any launch."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    n, count = 256, 1
+    A, dens, S = _case(n, count, 15)
+    d, s, a = _device_arrays(torch, A, dens, S)
+    raw = torch.zeros(2 * n * n * count + 2, dtype=torch.float32, device=dev)
+    odd = raw[2:]
+    assert odd.data_ptr() % 16 == 8
+    with pytest.raises(_lib.EngineError) as ei:
+        _call(n, odd, s, a, count, _lib.SPE_OP_ER, 1, 0.0, 0.0, torch.cuda.current_stream(dev))
+    assert ei.value.code == 1 and "16-byte" in str(ei.value)
