@@ -17,7 +17,8 @@
 // then the primes), with the twiddles of a table exp(2 pi i m / n) computed
 // in double and held in shared memory.  Radices 2, 3, 4, 5, 7 and 8 run as
 // butterflies in registers (a thread reads the R inputs of one butterfly,
-// applies its twiddles and the radix-R DFT, writes R outputs); a larger prime
+// applies its twiddles and the radix-R DFT, writes R outputs), and so do the
+// primes 11 .. 31, with the symmetric form of the prime DFT; a larger prime
 // radix computes each output as the direct sum over its R inputs with the
 // combined twiddle
 //   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)),
@@ -43,6 +44,7 @@ struct AnyPlan {
   int LS;                 // shared-memory stride of a line (odd: conflict-free 8-byte columns)
   int nrad;               // radix passes
   int rad[kMaxRadices];   // radices in pass order
+  int big;                // a radix among the primes 11 .. 31 (butterflies of any_pass_prime)
 };
 
 // Radix-R DFT of R registers with compile-time twiddles, R = 5 or 7 (the
@@ -110,6 +112,78 @@ __device__ __forceinline__ void any_pass_r(const float2* cur, float2* oth, const
   }
 }
 
+// Radix-R DFT of an odd prime R in its symmetric form (the terms r and R-r
+// paired): with a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r}, r = 1 .. (R-1)/2,
+//   X_0 = x_0 + sum_r a_r,
+//   X_q = A_q + i B_q,  X_{R-q} = A_q - i B_q,  q = 1 .. (R-1)/2,
+//   A_q = x_0 + sum_r a_r cos(2 pi r q / R),  B_q = sum_r b_r S sin(2 pi r q / R),
+// with the cosines and sines compile-time constants: (R-1)^2 real
+// multiply-adds for the R outputs, against 4 (R-1)^2 for the direct sums.
+// Output q goes to dst[q * NS] as soon as it is formed, so only the a_r,
+// b_r and one output pair are live.
+template <int R, int S, int Q, int RR>
+__device__ __forceinline__ void odd_sym_terms(const float2* a, const float2* b, float2& A, float2& B) {
+  if constexpr (RR <= (R - 1) / 2) {
+    constexpr float c = float(ct_cos_frac(RR * Q, R));
+    constexpr float s = float(S * ct_sin_frac(RR * Q, R));
+    A.x = fmaf(a[RR - 1].x, c, A.x);
+    A.y = fmaf(a[RR - 1].y, c, A.y);
+    B.x = fmaf(b[RR - 1].x, s, B.x);
+    B.y = fmaf(b[RR - 1].y, s, B.y);
+    odd_sym_terms<R, S, Q, RR + 1>(a, b, A, B);
+  }
+}
+template <int R, int S, int Q>
+__device__ __forceinline__ void odd_sym_outputs(const float2* a, const float2* b, float2 x0, float2* dst, int NS) {
+  if constexpr (Q <= (R - 1) / 2) {
+    float2 A = x0, B = make_float2(0.f, 0.f);
+    odd_sym_terms<R, S, Q, 1>(a, b, A, B);
+    dst[Q * NS] = make_float2(A.x - B.y, A.y + B.x);
+    dst[(R - Q) * NS] = make_float2(A.x + B.y, A.y - B.x);
+    odd_sym_outputs<R, S, Q + 1>(a, b, x0, dst, NS);
+  }
+}
+
+// One Stockham pass of an odd prime radix R (11 .. 31) as butterflies: the
+// inputs and twiddles of any_pass_r, the symmetric DFT above.  Not inlined:
+// one copy per (R, S) serves every operation's pass kernel.
+template <int R, int S>
+__device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw,
+                                            int nl, int NS) {
+  constexpr int H = (R - 1) / 2;
+  const int n = pl.n, LS = pl.LS, m = n / R, tstep = n / (NS * R);
+  for (int i = threadIdx.x; i < nl * m; i += kAnyThreads) {
+    const int c = i / m, b = i - c * m;
+    const int k = b % NS;
+    const float2* src = cur + c * LS + b;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[r * m];
+    if (NS > 1) {
+      const int e = k * tstep;  // < n / R
+      int idx = 0;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        idx += e;
+        float2 w = tw[idx];
+        if (S < 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    float2 sa[H], sb[H];
+    float2 x0 = v[0], sum = v[0];
+#pragma unroll
+    for (int r = 1; r <= H; ++r) {
+      sa[r - 1] = cadd(v[r], v[R - r]);
+      sb[r - 1] = csub(v[r], v[R - r]);
+      sum = cadd(sum, sa[r - 1]);
+    }
+    float2* dst = oth + c * LS + (b / NS) * NS * R + k;
+    dst[0] = sum;
+    odd_sym_outputs<R, S, 1>(sa, sb, x0, dst, NS);
+  }
+}
+
 // One pass of any other (prime) radix: each output as the direct sum over
 // its R inputs with the combined twiddle
 //   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)).
@@ -143,7 +217,10 @@ __device__ __forceinline__ void any_pass_generic(const float2* cur, float2* oth,
 
 // The transform of the tile's nl lines: one pass per radix of the plan,
 // ping-ponging between the two line buffers; on return `cur` holds it.
-template <int S>
+// BIG: the plan has a radix among the primes 11 .. 31, whose butterfly
+// functions need more registers than the rest; kernels without them are
+// compiled separately so that other sides keep their occupancy.
+template <int S, bool BIG>
 __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPlan& pl, const float2* tw, int nl) {
   int NS = 1;
   for (int ps = 0; ps < pl.nrad; ++ps) {
@@ -155,7 +232,22 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
       case 5: any_pass_r<5, S>(cur, oth, pl, tw, nl, NS); break;
       case 7: any_pass_r<7, S>(cur, oth, pl, tw, nl, NS); break;
       case 8: any_pass_r<8, S>(cur, oth, pl, tw, nl, NS); break;
-      default: any_pass_generic<S>(cur, oth, pl, tw, nl, NS, R); break;
+      default:
+        if constexpr (BIG) {
+          switch (R) {
+            case 11: any_pass_prime<11, S>(cur, oth, pl, tw, nl, NS); break;
+            case 13: any_pass_prime<13, S>(cur, oth, pl, tw, nl, NS); break;
+            case 17: any_pass_prime<17, S>(cur, oth, pl, tw, nl, NS); break;
+            case 19: any_pass_prime<19, S>(cur, oth, pl, tw, nl, NS); break;
+            case 23: any_pass_prime<23, S>(cur, oth, pl, tw, nl, NS); break;
+            case 29: any_pass_prime<29, S>(cur, oth, pl, tw, nl, NS); break;
+            case 31: any_pass_prime<31, S>(cur, oth, pl, tw, nl, NS); break;
+            default: any_pass_generic<S>(cur, oth, pl, tw, nl, NS, R); break;
+          }
+        } else {
+          any_pass_generic<S>(cur, oth, pl, tw, nl, NS, R);
+        }
+        break;
     }
     __syncthreads();
     float2* t = cur;
@@ -165,7 +257,7 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
   }
 }
 
-template <int AXIS, class Op>
+template <int AXIS, class Op, bool BIG>
 __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPlan pl, const float2* __restrict__ tw) {
   extern __shared__ float2 sm_any[];
   const int n = pl.n, W = pl.W, LS = pl.LS;
@@ -201,7 +293,7 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
     cur[c * LS + l] = op.load(base + (size_t)y * n + x, p, y, x, acc);
   }
   __syncthreads();
-  if constexpr (Op::FFT1 != 0) fft_any<Op::FFT1>(cur, oth, pl, tws, nl);
+  if constexpr (Op::FFT1 != 0) fft_any<Op::FFT1, BIG>(cur, oth, pl, tws, nl);
   if constexpr (Op::FFT2 != 0) {
     for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
       int c, l, y, x;
@@ -209,7 +301,7 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
       cur[c * LS + l] = op.mid(cur[c * LS + l], base + (size_t)y * n + x, p, y, x, acc);
     }
     __syncthreads();
-    fft_any<Op::FFT2>(cur, oth, pl, tws, nl);
+    fft_any<Op::FFT2, BIG>(cur, oth, pl, tws, nl);
   }
   for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
     int c, l, y, x;
@@ -250,6 +342,8 @@ bool make_plan(int n, AnyPlan& pl) {
     }
   }
   if (m != 1) return false;
+  pl.big = 0;
+  for (int i = 0; i < pl.nrad; ++i) pl.big |= (pl.rad[i] >= 11 && pl.rad[i] <= 31) ? 1 : 0;
   pl.LS = n | 1;
   const size_t table = (size_t)n * sizeof(float2);
   const size_t per_line = 2 * (size_t)pl.LS * sizeof(float2);
@@ -274,9 +368,9 @@ const AnyPlan& plan_of(int n) {
 
 size_t smem_of(const AnyPlan& pl) { return (2 * (size_t)pl.W * pl.LS + pl.n) * sizeof(float2); }
 
-template <int AXIS, class Op>
-cudaError_t launch_any(const Op& op, const AnyPlan& pl, int count, cudaStream_t st, const float2* tw) {
-  auto kern = pass_any<AXIS, Op>;
+template <int AXIS, class Op, bool BIG>
+cudaError_t launch_any_k(const Op& op, const AnyPlan& pl, int count, cudaStream_t st, const float2* tw) {
+  auto kern = pass_any<AXIS, Op, BIG>;
   static std::atomic<unsigned long long> configured{0ull};
   const size_t smem = smem_of(pl);
   // the attribute is set to the largest budget once: it is an upper bound
@@ -285,6 +379,11 @@ cudaError_t launch_any(const Op& op, const AnyPlan& pl, int count, cudaStream_t 
   const int tpi = (pl.n + pl.W - 1) / pl.W;
   kern<<<(unsigned)count * tpi, kAnyThreads, smem, st>>>(op, pl, tw);
   return cudaGetLastError();
+}
+template <int AXIS, class Op>
+cudaError_t launch_any(const Op& op, const AnyPlan& pl, int count, cudaStream_t st, const float2* tw) {
+  return pl.big ? launch_any_k<AXIS, Op, true>(op, pl, count, st, tw)
+                : launch_any_k<AXIS, Op, false>(op, pl, count, st, tw);
 }
 
 // ---------------------------------------------------------------------------

@@ -5,12 +5,14 @@ The reference plans any side (cufftPlan2d(n, n), src/gpu/gpu_context.h:29)
 and its front end produces arbitrary ones: by default the pattern is cropped
 to max(shape) (spring/pattern_manager.py:61-66), so the reference's own
 1054 x 1024 example patterns run at 1054 = 2 x 17 x 31.  Sides here: 1054;
-294 = 2 x 3 x 7^2; 100 = 4 x 5^2; 243 = 3^5; 97 (prime).
+294 = 2 x 3 x 7^2; 100 = 4 x 5^2; 243 = 3^5; 97 (a prime above 31: direct
+sums); and, for the symmetric prime butterflies, 286 = 2 x 11 x 13,
+874 = 2 x 19 x 23 and 116 = 4 x 29.
 
 Tolerances as for the compiled sides (test_gpu_parity.py): round trip,
 forward transform and projection 2e-6 relative L2, except 5e-6 where a
-radix-31 pass sums 31 products per output (1054); one iteration 2e-6 (5e-6
-at 1054); five iterations median 1e-4 (ER 2e-5), each individual 1e-2;
+pass of a prime radix from 11 sums up to 31 products per output; one
+iteration the same; five iterations median 1e-4 (ER 2e-5), each individual 1e-2;
 metrics 1e-5 / 1e-4; shrink-wrap supports identical except at pixels within
 1e-4 of the cut.
 """
@@ -22,11 +24,11 @@ from s_spi_spring_gb300 import _lib, synthetic
 
 pytestmark = pytest.mark.gpu
 
-SIDES = [1054, 294, 100, 243, 97]
+SIDES = [1054, 294, 100, 243, 97, 286, 874, 116]
 
 
 def tol1(n):
-    return 5e-6 if n == 1054 else 2e-6
+    return 5e-6 if n in (1054, 286, 874, 116) else 2e-6
 
 
 def rel(a, b):
@@ -76,7 +78,7 @@ def test_projection(n):
         assert rel(got[i], ref) < tol1(n), (n, i, rel(got[i], ref))
 
 
-@pytest.mark.parametrize("n", [1054, 294, 97])
+@pytest.mark.parametrize("n", [1054, 294, 97, 286, 874])
 @pytest.mark.parametrize("alg,beta,reality", [("HIO", 0.9, 0.0), ("RAAR", 0.87, 0.0), ("ER", 0.0, 0.5)])
 def test_iterations(n, alg, beta, reality):
     A, dens, S = case(n, 3, n + 2)
