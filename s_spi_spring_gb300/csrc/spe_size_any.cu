@@ -45,7 +45,20 @@ struct AnyPlan {
   int nrad;               // radix passes
   int rad[kMaxRadices];   // radices in pass order
   int big;                // a radix among the primes 11 .. 31 (butterflies of any_pass_prime)
+  // divisors of the index arithmetic as fast-division constants (fdiv):
+  // the side, and per pass the butterflies per line n / R, the stride NS of
+  // the pass's outputs and the span NS * R of its sub-transforms
+  unsigned inv_n;
+  int ns[kMaxRadices];
+  unsigned inv_m[kMaxRadices], inv_ns[kMaxRadices], inv_span[kMaxRadices];
 };
+
+// x / d as one multiply-high, inv = ceil(2^32 / d) (0 encodes d = 1).  Exact
+// for x < 2^17 and d < 2^15: with x = q d + s and inv d = 2^32 + r, r < d,
+// x inv / 2^32 = q + (s + x r / 2^32) / d, and s + x r / 2^32 < d.  Every
+// index divided here is below W n <= 8 * 14079 < 2^17 (make_plan checks).
+__host__ __device__ constexpr unsigned fdiv_inv(int d) { return d <= 1 ? 0u : 0xFFFFFFFFu / (unsigned)d + 1u; }
+__device__ __forceinline__ int fdiv(int x, unsigned inv) { return inv ? (int)__umulhi((unsigned)x, inv) : x; }
 
 // Radix-R DFT of R registers with compile-time twiddles, R = 5 or 7 (the
 // other radices of the butterfly passes use dft<R, S> of spe_fft.cuh):
@@ -85,11 +98,12 @@ __device__ __forceinline__ void small_dft(float2* v) {
 // outputs at (b/NS) NS R + k + q NS.
 template <int R, int S>
 __device__ __forceinline__ void any_pass_r(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw, int nl,
-                                           int NS) {
-  const int n = pl.n, LS = pl.LS, m = n / R, tstep = n / (NS * R);
+                                           int ps) {
+  const int n = pl.n, LS = pl.LS, m = n / R, NS = pl.ns[ps], tstep = n / (NS * R);
+  const unsigned inv_m = pl.inv_m[ps], inv_ns = pl.inv_ns[ps];
   for (int i = threadIdx.x; i < nl * m; i += kAnyThreads) {
-    const int c = i / m, b = i - c * m;
-    const int k = b % NS;
+    const int c = fdiv(i, inv_m), b = i - c * m;
+    const int bq = fdiv(b, inv_ns), k = b - bq * NS;
     const float2* src = cur + c * LS + b;
     float2 v[R];
 #pragma unroll
@@ -106,7 +120,7 @@ __device__ __forceinline__ void any_pass_r(const float2* cur, float2* oth, const
       }
     }
     small_dft<R, S>(v);
-    float2* dst = oth + c * LS + (b / NS) * NS * R + k;
+    float2* dst = oth + c * LS + bq * NS * R + k;
 #pragma unroll
     for (int q = 0; q < R; ++q) dst[q * NS] = v[q];
   }
@@ -149,12 +163,13 @@ __device__ __forceinline__ void odd_sym_outputs(const float2* a, const float2* b
 // one copy per (R, S) serves every operation's pass kernel.
 template <int R, int S>
 __device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw,
-                                            int nl, int NS) {
+                                            int nl, int ps) {
   constexpr int H = (R - 1) / 2;
-  const int n = pl.n, LS = pl.LS, m = n / R, tstep = n / (NS * R);
+  const int n = pl.n, LS = pl.LS, m = n / R, NS = pl.ns[ps], tstep = n / (NS * R);
+  const unsigned inv_m = pl.inv_m[ps], inv_ns = pl.inv_ns[ps];
   for (int i = threadIdx.x; i < nl * m; i += kAnyThreads) {
-    const int c = i / m, b = i - c * m;
-    const int k = b % NS;
+    const int c = fdiv(i, inv_m), b = i - c * m;
+    const int bq = fdiv(b, inv_ns), k = b - bq * NS;
     const float2* src = cur + c * LS + b;
     float2 v[R];
 #pragma unroll
@@ -178,7 +193,7 @@ __device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, cons
       sb[r - 1] = csub(v[r], v[R - r]);
       sum = cadd(sum, sa[r - 1]);
     }
-    float2* dst = oth + c * LS + (b / NS) * NS * R + k;
+    float2* dst = oth + c * LS + bq * NS * R + k;
     dst[0] = sum;
     odd_sym_outputs<R, S, 1>(sa, sb, x0, dst, NS);
   }
@@ -189,15 +204,15 @@ __device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, cons
 //   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)).
 template <int S>
 __device__ __forceinline__ void any_pass_generic(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw,
-                                                 int nl, int NS, int R) {
-  const int n = pl.n, LS = pl.LS;
+                                                 int nl, int ps, int R) {
+  const int n = pl.n, LS = pl.LS, NS = pl.ns[ps];
   const int m = n / R;        // butterflies; input stride
   const int span = NS * R;    // outputs of one sub-transform
   const int tstep = n / span; // twiddle-table step of one unit of (k + q NS)
   for (int i = threadIdx.x; i < nl * n; i += kAnyThreads) {
-    const int c = i / n, pos = i - c * n;
-    const int j = pos / span, rem = pos - j * span;
-    const int q = rem / NS, k = rem - q * NS;
+    const int c = fdiv(i, pl.inv_n), pos = i - c * n;
+    const int j = fdiv(pos, pl.inv_span[ps]), rem = pos - j * span;
+    const int q = fdiv(rem, pl.inv_ns[ps]), k = rem - q * NS;
     const float2* src = cur + c * LS + j * NS + k;
     const int e = (k + q * NS) * tstep;  // < n
     float2 acc = src[0];
@@ -222,30 +237,29 @@ __device__ __forceinline__ void any_pass_generic(const float2* cur, float2* oth,
 // compiled separately so that other sides keep their occupancy.
 template <int S, bool BIG>
 __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPlan& pl, const float2* tw, int nl) {
-  int NS = 1;
   for (int ps = 0; ps < pl.nrad; ++ps) {
     const int R = pl.rad[ps];
     switch (R) {
-      case 2: any_pass_r<2, S>(cur, oth, pl, tw, nl, NS); break;
-      case 3: any_pass_r<3, S>(cur, oth, pl, tw, nl, NS); break;
-      case 4: any_pass_r<4, S>(cur, oth, pl, tw, nl, NS); break;
-      case 5: any_pass_r<5, S>(cur, oth, pl, tw, nl, NS); break;
-      case 7: any_pass_r<7, S>(cur, oth, pl, tw, nl, NS); break;
-      case 8: any_pass_r<8, S>(cur, oth, pl, tw, nl, NS); break;
+      case 2: any_pass_r<2, S>(cur, oth, pl, tw, nl, ps); break;
+      case 3: any_pass_r<3, S>(cur, oth, pl, tw, nl, ps); break;
+      case 4: any_pass_r<4, S>(cur, oth, pl, tw, nl, ps); break;
+      case 5: any_pass_r<5, S>(cur, oth, pl, tw, nl, ps); break;
+      case 7: any_pass_r<7, S>(cur, oth, pl, tw, nl, ps); break;
+      case 8: any_pass_r<8, S>(cur, oth, pl, tw, nl, ps); break;
       default:
         if constexpr (BIG) {
           switch (R) {
-            case 11: any_pass_prime<11, S>(cur, oth, pl, tw, nl, NS); break;
-            case 13: any_pass_prime<13, S>(cur, oth, pl, tw, nl, NS); break;
-            case 17: any_pass_prime<17, S>(cur, oth, pl, tw, nl, NS); break;
-            case 19: any_pass_prime<19, S>(cur, oth, pl, tw, nl, NS); break;
-            case 23: any_pass_prime<23, S>(cur, oth, pl, tw, nl, NS); break;
-            case 29: any_pass_prime<29, S>(cur, oth, pl, tw, nl, NS); break;
-            case 31: any_pass_prime<31, S>(cur, oth, pl, tw, nl, NS); break;
-            default: any_pass_generic<S>(cur, oth, pl, tw, nl, NS, R); break;
+            case 11: any_pass_prime<11, S>(cur, oth, pl, tw, nl, ps); break;
+            case 13: any_pass_prime<13, S>(cur, oth, pl, tw, nl, ps); break;
+            case 17: any_pass_prime<17, S>(cur, oth, pl, tw, nl, ps); break;
+            case 19: any_pass_prime<19, S>(cur, oth, pl, tw, nl, ps); break;
+            case 23: any_pass_prime<23, S>(cur, oth, pl, tw, nl, ps); break;
+            case 29: any_pass_prime<29, S>(cur, oth, pl, tw, nl, ps); break;
+            case 31: any_pass_prime<31, S>(cur, oth, pl, tw, nl, ps); break;
+            default: any_pass_generic<S>(cur, oth, pl, tw, nl, ps, R); break;
           }
         } else {
-          any_pass_generic<S>(cur, oth, pl, tw, nl, NS, R);
+          any_pass_generic<S>(cur, oth, pl, tw, nl, ps, R);
         }
         break;
     }
@@ -253,7 +267,6 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
     float2* t = cur;
     cur = oth;
     oth = t;
-    NS *= R;
   }
 }
 
@@ -271,17 +284,18 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
   const int nl = min(W, n - l0);
   const size_t base = (size_t)p * n * n;
   const int tot = nl * n;
+  const unsigned inv_nl = fdiv_inv(nl);
   typename Op::Acc acc;
   // element i of the tile: row passes walk along x (whole rows), column
   // passes across the tile's columns first (row segments of nl elements)
   auto coords = [&](int i, int& c, int& l, int& y, int& x) {
     if (AXIS == AX_ROWS) {
-      c = i / n;
+      c = fdiv(i, pl.inv_n);
       l = i - c * n;
       y = l0 + c;
       x = l;
     } else {
-      l = i / nl;
+      l = fdiv(i, inv_nl);
       c = i - l * nl;
       y = l;
       x = l0 + c;
@@ -343,14 +357,24 @@ bool make_plan(int n, AnyPlan& pl) {
   }
   if (m != 1) return false;
   pl.big = 0;
-  for (int i = 0; i < pl.nrad; ++i) pl.big |= (pl.rad[i] >= 11 && pl.rad[i] <= 31) ? 1 : 0;
+  pl.inv_n = fdiv_inv(n);
+  for (int i = 0, ns = 1; i < pl.nrad; ns *= pl.rad[i], ++i) {
+    pl.big |= (pl.rad[i] >= 11 && pl.rad[i] <= 31) ? 1 : 0;
+    pl.ns[i] = ns;
+    pl.inv_m[i] = fdiv_inv(n / pl.rad[i]);
+    pl.inv_ns[i] = fdiv_inv(ns);
+    pl.inv_span[i] = fdiv_inv(ns * pl.rad[i]);
+  }
   pl.LS = n | 1;
   const size_t table = (size_t)n * sizeof(float2);
   const size_t per_line = 2 * (size_t)pl.LS * sizeof(float2);
   if (table + per_line > kAnySmem) return false;
   const size_t w = (kAnySmem - table) / per_line;
   pl.W = (int)(w < 8 ? w : 8);
-  return true;
+  // the bounds of fdiv: indices below W n < 2^17, divisors below 2^15
+  if (n >= (1 << 15)) return false;
+  while (pl.W > 1 && (size_t)pl.W * n >= (1u << 17)) --pl.W;
+  return (size_t)pl.W * n < (1u << 17);
 }
 
 struct AnyEntry {
