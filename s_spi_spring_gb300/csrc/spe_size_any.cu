@@ -33,7 +33,8 @@
 namespace spe {
 namespace {
 
-constexpr int kAnyThreads = 512;
+constexpr int kAnyThreads = 512;     // threads of a pass CTA
+constexpr int kAnyThreadsBig = 256;  // the same for plans with a prime radix 11 .. 31 (128 registers each)
 constexpr int kMaxPrime = 257;       // largest prime factor accepted
 constexpr int kMaxRadices = 24;
 constexpr size_t kAnySmem = 220 * 1024;  // shared-memory budget of one CTA (two line buffers)
@@ -96,12 +97,12 @@ __device__ __forceinline__ void small_dft(float2* v) {
 // inputs x[b + r n/R] of a butterfly, multiplies them by w_{NS R}^{k r}
 // (k = b mod NS), runs the radix-R DFT in registers and writes its R
 // outputs at (b/NS) NS R + k + q NS.
-template <int R, int S>
+template <int R, int S, int NT>
 __device__ __forceinline__ void any_pass_r(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw, int nl,
                                            int ps) {
   const int n = pl.n, LS = pl.LS, m = n / R, NS = pl.ns[ps], tstep = n / (NS * R);
   const unsigned inv_m = pl.inv_m[ps], inv_ns = pl.inv_ns[ps];
-  for (int i = threadIdx.x; i < nl * m; i += kAnyThreads) {
+  for (int i = threadIdx.x; i < nl * m; i += NT) {
     const int c = fdiv(i, inv_m), b = i - c * m;
     const int bq = fdiv(b, inv_ns), k = b - bq * NS;
     const float2* src = cur + c * LS + b;
@@ -167,7 +168,7 @@ __device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, cons
   constexpr int H = (R - 1) / 2;
   const int n = pl.n, LS = pl.LS, m = n / R, NS = pl.ns[ps], tstep = n / (NS * R);
   const unsigned inv_m = pl.inv_m[ps], inv_ns = pl.inv_ns[ps];
-  for (int i = threadIdx.x; i < nl * m; i += kAnyThreads) {
+  for (int i = threadIdx.x; i < nl * m; i += kAnyThreadsBig) {
     const int c = fdiv(i, inv_m), b = i - c * m;
     const int bq = fdiv(b, inv_ns), k = b - bq * NS;
     const float2* src = cur + c * LS + b;
@@ -202,14 +203,14 @@ __device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, cons
 // One pass of any other (prime) radix: each output as the direct sum over
 // its R inputs with the combined twiddle
 //   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)).
-template <int S>
+template <int S, int NT>
 __device__ __forceinline__ void any_pass_generic(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw,
                                                  int nl, int ps, int R) {
   const int n = pl.n, LS = pl.LS, NS = pl.ns[ps];
   const int m = n / R;        // butterflies; input stride
   const int span = NS * R;    // outputs of one sub-transform
   const int tstep = n / span; // twiddle-table step of one unit of (k + q NS)
-  for (int i = threadIdx.x; i < nl * n; i += kAnyThreads) {
+  for (int i = threadIdx.x; i < nl * n; i += NT) {
     const int c = fdiv(i, pl.inv_n), pos = i - c * n;
     const int j = fdiv(pos, pl.inv_span[ps]), rem = pos - j * span;
     const int q = fdiv(rem, pl.inv_ns[ps]), k = rem - q * NS;
@@ -235,17 +236,17 @@ __device__ __forceinline__ void any_pass_generic(const float2* cur, float2* oth,
 // BIG: the plan has a radix among the primes 11 .. 31, whose butterfly
 // functions need more registers than the rest; kernels without them are
 // compiled separately so that other sides keep their occupancy.
-template <int S, bool BIG>
+template <int S, bool BIG, int NT = BIG ? kAnyThreadsBig : kAnyThreads>
 __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPlan& pl, const float2* tw, int nl) {
   for (int ps = 0; ps < pl.nrad; ++ps) {
     const int R = pl.rad[ps];
     switch (R) {
-      case 2: any_pass_r<2, S>(cur, oth, pl, tw, nl, ps); break;
-      case 3: any_pass_r<3, S>(cur, oth, pl, tw, nl, ps); break;
-      case 4: any_pass_r<4, S>(cur, oth, pl, tw, nl, ps); break;
-      case 5: any_pass_r<5, S>(cur, oth, pl, tw, nl, ps); break;
-      case 7: any_pass_r<7, S>(cur, oth, pl, tw, nl, ps); break;
-      case 8: any_pass_r<8, S>(cur, oth, pl, tw, nl, ps); break;
+      case 2: any_pass_r<2, S, NT>(cur, oth, pl, tw, nl, ps); break;
+      case 3: any_pass_r<3, S, NT>(cur, oth, pl, tw, nl, ps); break;
+      case 4: any_pass_r<4, S, NT>(cur, oth, pl, tw, nl, ps); break;
+      case 5: any_pass_r<5, S, NT>(cur, oth, pl, tw, nl, ps); break;
+      case 7: any_pass_r<7, S, NT>(cur, oth, pl, tw, nl, ps); break;
+      case 8: any_pass_r<8, S, NT>(cur, oth, pl, tw, nl, ps); break;
       default:
         if constexpr (BIG) {
           switch (R) {
@@ -256,10 +257,10 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
             case 23: any_pass_prime<23, S>(cur, oth, pl, tw, nl, ps); break;
             case 29: any_pass_prime<29, S>(cur, oth, pl, tw, nl, ps); break;
             case 31: any_pass_prime<31, S>(cur, oth, pl, tw, nl, ps); break;
-            default: any_pass_generic<S>(cur, oth, pl, tw, nl, ps, R); break;
+            default: any_pass_generic<S, NT>(cur, oth, pl, tw, nl, ps, R); break;
           }
         } else {
-          any_pass_generic<S>(cur, oth, pl, tw, nl, ps, R);
+          any_pass_generic<S, NT>(cur, oth, pl, tw, nl, ps, R);
         }
         break;
     }
@@ -271,13 +272,15 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
 }
 
 template <int AXIS, class Op, bool BIG>
-__global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPlan pl, const float2* __restrict__ tw) {
+__global__ void __launch_bounds__(BIG ? kAnyThreadsBig : kAnyThreads)
+    pass_any(const Op op, const AnyPlan pl, const float2* __restrict__ tw) {
+  constexpr int NT = BIG ? kAnyThreadsBig : kAnyThreads;
   extern __shared__ float2 sm_any[];
   const int n = pl.n, W = pl.W, LS = pl.LS;
   float2* cur = sm_any;
   float2* oth = sm_any + (size_t)W * LS;
   float2* tws = sm_any + (size_t)2 * W * LS;  // the twiddle table, n entries
-  for (int i = threadIdx.x; i < n; i += kAnyThreads) tws[i] = __ldg(tw + i);
+  for (int i = threadIdx.x; i < n; i += NT) tws[i] = __ldg(tw + i);
   const int tpi = (n + W - 1) / W;
   const int p = op.first + blockIdx.x / tpi;
   const int l0 = (blockIdx.x % tpi) * W;
@@ -301,7 +304,7 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
       x = l0 + c;
     }
   };
-  for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
+  for (int i = threadIdx.x; i < tot; i += NT) {
     int c, l, y, x;
     coords(i, c, l, y, x);
     cur[c * LS + l] = op.load(base + (size_t)y * n + x, p, y, x, acc);
@@ -309,7 +312,7 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
   __syncthreads();
   if constexpr (Op::FFT1 != 0) fft_any<Op::FFT1, BIG>(cur, oth, pl, tws, nl);
   if constexpr (Op::FFT2 != 0) {
-    for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
+    for (int i = threadIdx.x; i < tot; i += NT) {
       int c, l, y, x;
       coords(i, c, l, y, x);
       cur[c * LS + l] = op.mid(cur[c * LS + l], base + (size_t)y * n + x, p, y, x, acc);
@@ -317,7 +320,7 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
     __syncthreads();
     fft_any<Op::FFT2, BIG>(cur, oth, pl, tws, nl);
   }
-  for (int i = threadIdx.x; i < tot; i += kAnyThreads) {
+  for (int i = threadIdx.x; i < tot; i += NT) {
     int c, l, y, x;
     coords(i, c, l, y, x);
     op.store(cur[c * LS + l], base + (size_t)y * n + x, p, y, x, acc);
@@ -325,9 +328,9 @@ __global__ void __launch_bounds__(kAnyThreads) pass_any(const Op op, const AnyPl
   if constexpr (Op::NSUM + Op::NMAX > 0) {
     double r[NRED];
     acc.values(r);
-    block_reduce_store<kAnyThreads, Op::NSUM, Op::NMAX>(op.partials, r);
+    block_reduce_store<NT, Op::NSUM, Op::NMAX>(op.partials, r);
   }
-  if constexpr (Op::PEAK) block_argmax_store<kAnyThreads>(op.partials, acc.mx, acc.idx);
+  if constexpr (Op::PEAK) block_argmax_store<NT>(op.partials, acc.mx, acc.idx);
 }
 
 // ---------------------------------------------------------------------------
@@ -369,7 +372,9 @@ bool make_plan(int n, AnyPlan& pl) {
   const size_t table = (size_t)n * sizeof(float2);
   const size_t per_line = 2 * (size_t)pl.LS * sizeof(float2);
   if (table + per_line > kAnySmem) return false;
-  const size_t w = (kAnySmem - table) / per_line;
+  // plans with a big prime run 256-thread CTAs, two per SM: half the budget
+  const size_t budget = (pl.big && table + per_line <= kAnySmem / 2) ? kAnySmem / 2 : kAnySmem;
+  const size_t w = (budget - table) / per_line;
   pl.W = (int)(w < 8 ? w : 8);
   // the bounds of fdiv: indices below W n < 2^17, divisors below 2^15
   if (n >= (1 << 15)) return false;
@@ -401,7 +406,7 @@ cudaError_t launch_any_k(const Op& op, const AnyPlan& pl, int count, cudaStream_
   cudaError_t e = configure(kern, kAnySmem, configured);
   if (e != cudaSuccess || count <= 0) return e;
   const int tpi = (pl.n + pl.W - 1) / pl.W;
-  kern<<<(unsigned)count * tpi, kAnyThreads, smem, st>>>(op, pl, tw);
+  kern<<<(unsigned)count * tpi, BIG ? kAnyThreadsBig : kAnyThreads, smem, st>>>(op, pl, tw);
   return cudaGetLastError();
 }
 template <int AXIS, class Op>
