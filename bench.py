@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--large-tune-iters", type=int, default=2,
                     help="iterations per autotuning trial of the 2048^2 x 128 population")
     ap.add_argument("--refine", type=int, default=1, help="time the gradient-refinement epoch (0: skip)")
+    ap.add_argument("--example-side", type=int, default=1,
+                    help="time side 1054 (no compiled plan) against the reference's kernels + cuFFT (0: skip)")
     ap.add_argument("--profile-loss", action="store_true", help="profiling case: one loss + gradient at 512^2 x 64")
     ap.add_argument("--profile-sizes", action="store_true",
                     help="profiling case: two RAAR iterations per pattern side 256..2048")
@@ -513,6 +515,56 @@ def large_population(args, local):
             "rfactor_median": round(float(np.median([x["error_fourier"] for x in m])), 5)}
 
 
+def example_side(args, local):
+    """Side 1054 = 2 x 17 x 31, the size the reference's front end gives its
+    own 1054 x 1024 example patterns (cropped to max(shape)): 16 individuals,
+    RAAR beta 0.87, 20-iteration calls, CUDA events, best of 3; the run-time
+    kernels of the sides without a compiled plan against the reference's own
+    compiled kernels with cuFFT in its 8-context structure, from the same
+    start."""
+    import torch
+    from s_spi_spring_gb300 import _lib, synthetic
+    n, P, iters = 1054, 16, 20
+    I, _, _ = synthetic.polygon_pattern(seed=3, n=n, diameter=n * 0.23, photons=1e8, stop_radius=max(2, n // 64))
+    A = _lib.prepare_pattern(I, (-1, -1), True)
+    dens, S = synthetic.start_population(n, P, n * 0.2, seed=4)
+    eng = _lib.Engine(n, local)
+    eng.set_amplitudes(A)
+    eng.upload(0, dens, S)
+    eng.raar(0, P, 2, BETA, 0.0)
+    eng.synchronize()
+    st = torch.cuda.ExternalStream(eng.get_stream(), device=f"cuda:{local}") if eng.get_stream() else \
+        torch.cuda.current_stream()
+    ts = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        eng.raar(0, P, iters, BETA, 0.0)
+        e1.record(st)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) / iters)
+    eng.close()
+    out = {"workload": "1054x1054 complex64 (2 x 17 x 31), 16 individuals, RAAR beta 0.87",
+           "engine_ms_per_iteration": round(min(ts), 4), "engine_iter_ind_per_s": round(P / (min(ts) / 1e3), 1)}
+    from baseline import plain, ref_kernels
+    if not ref_kernels.available():
+        out["reference_gpu_kernels"] = "unavailable (the reference's kernels were not compiled)"
+        return out
+    pl = plain.Plain(A, nctx=8, device=local, kernels="reference")
+    d_rho = torch.from_numpy(dens.view(np.float32).copy()).to(f"cuda:{local}")
+    d_S = torch.from_numpy(S.copy()).to(f"cuda:{local}")
+    pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), P, 2, 1, BETA, 0.0, copies=False)
+    tp = []
+    for _ in range(3):
+        pl.iterate(d_rho.data_ptr(), d_S.data_ptr(), P, iters, 1, BETA, 0.0, copies=False)
+        tp.append(pl.last_ms() / iters)
+    pl.close()
+    out.update({"reference_ms_per_iteration": round(min(tp), 4),
+                "reference_iter_ind_per_s": round(P / (min(tp) / 1e3), 1),
+                "engine_over_reference": round(min(tp) / min(ts), 2)})
+    return out
+
+
 def large_memetic(args, local):
     """The large-population workload as specified, over a bounded number of
     generations: 2048 x 2048, 128 individuals; per generation shrink-wrap,
@@ -743,6 +795,11 @@ def run_engine(args):
             out["large_memetic"] = large_memetic(args, local)
         except Exception as ex:
             out["large_memetic"] = {"error": str(ex)[:300]}
+    if rank == 0 and args.example_side:
+        try:
+            out["example_side"] = example_side(args, local)
+        except Exception as ex:
+            out["example_side"] = {"error": str(ex)[:300]}
     if rank == 0 and args.refine:
         try:
             out["refinement"] = refinement(args, local)
