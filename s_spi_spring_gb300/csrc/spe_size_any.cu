@@ -19,11 +19,9 @@
 // butterflies in registers (a thread reads the R inputs of one butterfly,
 // applies its twiddles and the radix-R DFT, writes R outputs), and so do the
 // primes 11 .. 31, with the symmetric form of the prime DFT; a larger prime
-// radix computes each output as the direct sum over its R inputs with the
-// combined twiddle
-//   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)),
-// k = b mod NS, R complex multiply-adds per point: sides whose largest prime
-// factor exceeds kMaxPrime are rejected rather than run at that cost.
+// radix runs the same symmetric form with run-time R over shared memory
+// (about R real multiply-adds per point): sides whose largest prime factor
+// exceeds kMaxPrime are rejected rather than run at that cost.
 #include <map>
 #include <memory>
 #include <mutex>
@@ -34,7 +32,7 @@ namespace spe {
 namespace {
 
 constexpr int kAnyThreads = 512;     // threads of a pass CTA
-constexpr int kAnyThreadsBig = 256;  // the same for plans with a prime radix 11 .. 31 (128 registers each)
+constexpr int kAnyThreadsBig = 256;  // the same for plans with a prime radix of 11 or more (128 registers each)
 constexpr int kMaxPrime = 257;       // largest prime factor accepted
 constexpr int kMaxRadices = 24;
 constexpr size_t kAnySmem = 220 * 1024;  // shared-memory budget of one CTA (two line buffers)
@@ -45,7 +43,7 @@ struct AnyPlan {
   int LS;                 // shared-memory stride of a line (odd: conflict-free 8-byte columns)
   int nrad;               // radix passes
   int rad[kMaxRadices];   // radices in pass order
-  int big;                // a radix among the primes 11 .. 31 (butterflies of any_pass_prime)
+  int big;                // a prime radix of 11 or more (any_pass_prime, any_pass_sym: the BIG kernels)
   // divisors of the index arithmetic as fast-division constants (fdiv):
   // the side, and per pass the butterflies per line n / R, the stride NS of
   // the pass's outputs and the span NS * R of its sub-transforms
@@ -200,42 +198,127 @@ __device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, cons
   }
 }
 
-// One pass of any other (prime) radix: each output as the direct sum over
-// its R inputs with the combined twiddle
-//   out[(b/NS) NS R + k + q NS] = sum_r x[b + r n/R] exp(S 2 pi i r (k + q NS) / (NS R)).
+// One pass of an odd prime radix above 31, in the symmetric form of the
+// prime DFT with run-time R (H = (R-1)/2), in two steps over shared memory:
+//   1. per butterfly and pair (r, R-r), r = 1 .. H: y_r = x_r w^{k r},
+//      y_{R-r} = x_{R-r} w^{k (R-r)} (the inter-pass twiddles), then
+//      a_r = y_r + y_{R-r} into slot r and b_r = y_r - y_{R-r} into slot R-r,
+//      in place (each element is read and written by one thread);
+//   2. per butterfly and q = 0 .. H: X_0 = y_0 + sum a_r, and for q >= 1
+//      X_q, X_{R-q} = A_q +- i B_q with A_q = y_0 + sum_r a_r cos(2 pi r q / R),
+//      B_q = sum_r b_r S sin(2 pi r q / R), the cosines and sines read from
+//      the side's table (exp(2 pi i t m / n) = exp(2 pi i t / R), m = n / R).
+// About 2 real multiply-adds per input and output pair instead of 4 per
+// input and output.
 template <int S, int NT>
-__device__ __forceinline__ void any_pass_generic(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw,
-                                                 int nl, int ps, int R) {
-  const int n = pl.n, LS = pl.LS, NS = pl.ns[ps];
-  const int m = n / R;        // butterflies; input stride
-  const int span = NS * R;    // outputs of one sub-transform
-  const int tstep = n / span; // twiddle-table step of one unit of (k + q NS)
-  for (int i = threadIdx.x; i < nl * n; i += NT) {
-    const int c = fdiv(i, pl.inv_n), pos = i - c * n;
-    const int j = fdiv(pos, pl.inv_span[ps]), rem = pos - j * span;
-    const int q = fdiv(rem, pl.inv_ns[ps]), k = rem - q * NS;
-    const float2* src = cur + c * LS + j * NS + k;
-    const int e = (k + q * NS) * tstep;  // < n
-    float2 acc = src[0];
-    int idx = 0;
-    for (int r = 1; r < R; ++r) {
-      idx += e;
-      if (idx >= n) idx -= n;
-      float2 w = tw[idx];
-      if (S < 0) w.y = -w.y;
-      const float2 x = src[r * m];
-      acc.x = fmaf(x.x, w.x, fmaf(-x.y, w.y, acc.x));
-      acc.y = fmaf(x.x, w.y, fmaf(x.y, w.x, acc.y));
+__device__ __noinline__ void any_pass_sym(float2* cur, float2* oth, const AnyPlan& pl, const float2* tw, int nl,
+                                          int ps, int R) {
+  const int n = pl.n, LS = pl.LS, NS = pl.ns[ps], H = (R - 1) / 2;
+  const int m = n / R, tstep = n / (NS * R);
+  const unsigned inv_m = pl.inv_m[ps], inv_ns = pl.inv_ns[ps];
+  const unsigned inv_h = fdiv_inv(H), inv_h1 = fdiv_inv(H + 1);
+  // 1. twiddles and pairs, in place
+  for (int i = threadIdx.x; i < nl * m * H; i += NT) {
+    const int u = fdiv(i, inv_h), r = 1 + (i - u * H);  // u: butterfly of the tile
+    const int c = fdiv(u, inv_m), b = u - c * m;
+    const int k = b - fdiv(b, inv_ns) * NS;
+    float2* src = cur + c * LS + b;
+    float2 x = src[r * m], y = src[(R - r) * m];
+    if (NS > 1) {
+      const int e = k * tstep;  // w^{k r} = table[e r]; e < n / R, so e r < n
+      float2 w1 = tw[e * r], w2 = tw[e * (R - r)];
+      if (S < 0) {
+        w1.y = -w1.y;
+        w2.y = -w2.y;
+      }
+      x = cmul(x, w1);
+      y = cmul(y, w2);
     }
-    oth[c * LS + pos] = acc;
+    src[r * m] = cadd(x, y);
+    src[(R - r) * m] = csub(x, y);
+  }
+  __syncthreads();
+  // 2. output pairs: QB values of q for BB butterflies per thread (each
+  // a_r, b_r load serves QB pairs, each table lookup BB butterflies); q = 0
+  // takes the table's exp(0) = 1 exactly: X_0 = y_0 + sum a_r
+  constexpr int QB = 4, BB = 2;
+  const int G = (H + QB) / QB;  // groups of q in [0, H]
+  const int nb = nl * m;        // butterflies of the tile
+  const unsigned inv_g = fdiv_inv(G);
+  for (int i = threadIdx.x; i < ((nb + BB - 1) / BB) * G; i += NT) {
+    const int up = fdiv(i, inv_g), g = i - up * G;
+    const float2* src[BB];
+    float2* dst[BB];
+    float2 y0[BB];
+    bool live[BB];
+#pragma unroll
+    for (int v = 0; v < BB; ++v) {
+      const int u0 = up * BB + v;
+      live[v] = u0 < nb;
+      const int u = live[v] ? u0 : up * BB;  // a tail slot repeats the first butterfly, unstored
+      const int c = fdiv(u, inv_m), b = u - c * m;
+      const int bq = fdiv(b, inv_ns), k = b - bq * NS;
+      src[v] = cur + c * LS + b;
+      dst[v] = oth + c * LS + bq * NS * R + k;
+      y0[v] = src[v][0];
+    }
+    float2 A[BB][QB], B[BB][QB];
+    int idx[QB], step[QB];
+#pragma unroll
+    for (int t = 0; t < QB; ++t) {
+      const int q = g * QB + t;
+      idx[t] = 0;
+      step[t] = q <= H ? q * m : 0;  // table index of exp(2 pi i r q / R) advances by q m mod n
+#pragma unroll
+      for (int v = 0; v < BB; ++v) {
+        A[v][t] = y0[v];
+        B[v][t] = make_float2(0.f, 0.f);
+      }
+    }
+    for (int r = 1; r <= H; ++r) {
+      float2 a[BB], bb[BB];
+#pragma unroll
+      for (int v = 0; v < BB; ++v) {
+        a[v] = src[v][r * m];
+        bb[v] = src[v][(R - r) * m];
+      }
+#pragma unroll
+      for (int t = 0; t < QB; ++t) {
+        idx[t] += step[t];
+        if (idx[t] >= n) idx[t] -= n;
+        const float2 w = tw[idx[t]];
+        const float ws = S < 0 ? -w.y : w.y;
+#pragma unroll
+        for (int v = 0; v < BB; ++v) {
+          A[v][t].x = fmaf(a[v].x, w.x, A[v][t].x);
+          A[v][t].y = fmaf(a[v].y, w.x, A[v][t].y);
+          B[v][t].x = fmaf(bb[v].x, ws, B[v][t].x);
+          B[v][t].y = fmaf(bb[v].y, ws, B[v][t].y);
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < BB; ++v) {
+      if (!live[v]) continue;
+#pragma unroll
+      for (int t = 0; t < QB; ++t) {
+        const int q = g * QB + t;
+        if (q == 0) {
+          dst[v][0] = A[v][t];
+        } else if (q <= H) {
+          dst[v][q * NS] = make_float2(A[v][t].x - B[v][t].y, A[v][t].y + B[v][t].x);
+          dst[v][(R - q) * NS] = make_float2(A[v][t].x + B[v][t].y, A[v][t].y - B[v][t].x);
+        }
+      }
+    }
   }
 }
 
 // The transform of the tile's nl lines: one pass per radix of the plan,
 // ping-ponging between the two line buffers; on return `cur` holds it.
-// BIG: the plan has a radix among the primes 11 .. 31, whose butterfly
-// functions need more registers than the rest; kernels without them are
-// compiled separately so that other sides keep their occupancy.
+// BIG: the plan has a prime radix of 11 or more, whose pass functions need
+// more registers than the rest; kernels without them are compiled
+// separately so that the other sides keep their occupancy.
 template <int S, bool BIG, int NT = BIG ? kAnyThreadsBig : kAnyThreads>
 __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPlan& pl, const float2* tw, int nl) {
   for (int ps = 0; ps < pl.nrad; ++ps) {
@@ -257,11 +340,11 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
             case 23: any_pass_prime<23, S>(cur, oth, pl, tw, nl, ps); break;
             case 29: any_pass_prime<29, S>(cur, oth, pl, tw, nl, ps); break;
             case 31: any_pass_prime<31, S>(cur, oth, pl, tw, nl, ps); break;
-            default: any_pass_generic<S, NT>(cur, oth, pl, tw, nl, ps, R); break;
+            default: any_pass_sym<S, NT>(cur, oth, pl, tw, nl, ps, R); break;
           }
-        } else {
-          any_pass_generic<S, NT>(cur, oth, pl, tw, nl, ps, R);
         }
+        // (kernels without BIG never see a radix of 11 or more: make_plan
+        // sends every such plan to the BIG kernels)
         break;
     }
     __syncthreads();
@@ -362,7 +445,7 @@ bool make_plan(int n, AnyPlan& pl) {
   pl.big = 0;
   pl.inv_n = fdiv_inv(n);
   for (int i = 0, ns = 1; i < pl.nrad; ns *= pl.rad[i], ++i) {
-    pl.big |= (pl.rad[i] >= 11 && pl.rad[i] <= 31) ? 1 : 0;
+    pl.big |= pl.rad[i] >= 11 ? 1 : 0;
     pl.ns[i] = ns;
     pl.inv_m[i] = fdiv_inv(n / pl.rad[i]);
     pl.inv_ns[i] = fdiv_inv(ns);

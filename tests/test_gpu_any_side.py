@@ -5,14 +5,16 @@ The reference plans any side (cufftPlan2d(n, n), src/gpu/gpu_context.h:29)
 and its front end produces arbitrary ones: by default the pattern is cropped
 to max(shape) (spring/pattern_manager.py:61-66), so the reference's own
 1054 x 1024 example patterns run at 1054 = 2 x 17 x 31.  Sides here: 1054;
-294 = 2 x 3 x 7^2; 100 = 4 x 5^2; 243 = 3^5; 97 (a prime above 31: direct
-sums); and, for the symmetric prime butterflies, 286 = 2 x 11 x 13,
-874 = 2 x 19 x 23 and 116 = 4 x 29.
+294 = 2 x 3 x 7^2; 100 = 4 x 5^2; 243 = 3^5; for the symmetric prime
+butterflies 286 = 2 x 11 x 13, 874 = 2 x 19 x 23 and 116 = 4 x 29; and for
+the run-time symmetric pass of primes above 31, 97 (prime) and
+1030 = 2 x 5 x 103 (a detector's side).
 
 Tolerances as for the compiled sides (test_gpu_parity.py): round trip,
 forward transform and projection 2e-6 relative L2, except 5e-6 where a
-pass of a prime radix from 11 sums up to 31 products per output; one
-iteration the same; five iterations median 1e-4 (ER 2e-5), each individual 1e-2;
+pass of a prime radix from 11 sums 5 to 51 products per output; one
+iteration the same; five iterations median 1e-4 (ER 2e-5), each individual
+1e-2 (gated ER 3e-2, as at side 2048: phase-gate decisions at the threshold);
 metrics 1e-5 / 1e-4; shrink-wrap supports identical except at pixels within
 1e-4 of the cut.
 """
@@ -24,11 +26,11 @@ from s_spi_spring_gb300 import _lib, synthetic
 
 pytestmark = pytest.mark.gpu
 
-SIDES = [1054, 294, 100, 243, 97, 286, 874, 116]
+SIDES = [1054, 294, 100, 243, 97, 286, 874, 116, 1030]
 
 
 def tol1(n):
-    return 5e-6 if n in (1054, 286, 874, 116) else 2e-6
+    return 5e-6 if n in (1054, 286, 874, 116, 1030) else 2e-6
 
 
 def rel(a, b):
@@ -78,12 +80,17 @@ def test_projection(n):
         assert rel(got[i], ref) < tol1(n), (n, i, rel(got[i], ref))
 
 
-@pytest.mark.parametrize("n", [1054, 294, 97, 286, 874])
+@pytest.mark.parametrize("n", [1054, 294, 97, 286, 874, 1030])
 @pytest.mark.parametrize("alg,beta,reality", [("HIO", 0.9, 0.0), ("RAAR", 0.87, 0.0), ("ER", 0.0, 0.5)])
 def test_iterations(n, alg, beta, reality):
     A, dens, S = case(n, 3, n + 2)
     e = engine(n, A, dens, S)
-    for iters, tol in ((1, tol1(n)), (5, 1e-2)):
+    # five iterations: 1e-2 per individual, 3e-2 for gated ER (reality > 0),
+    # where a pixel's phase-gate decision within rounding of the threshold
+    # can flip between FP32 and FP64 and the difference grows over the
+    # iterations (as at side 2048); the median bound below stays strict
+    five = 3e-2 if (alg == "ER" and reality > 0) else 1e-2
+    for iters, tol in ((1, tol1(n)), (5, five)):
         e.upload(0, dens, S)
         if alg == "HIO":
             e.hio(0, 3, iters, beta, reality)
