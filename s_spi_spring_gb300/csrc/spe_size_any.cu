@@ -59,33 +59,51 @@ struct AnyPlan {
 __host__ __device__ constexpr unsigned fdiv_inv(int d) { return d <= 1 ? 0u : 0xFFFFFFFFu / (unsigned)d + 1u; }
 __device__ __forceinline__ int fdiv(int x, unsigned inv) { return inv ? (int)__umulhi((unsigned)x, inv) : x; }
 
-// Radix-R DFT of R registers with compile-time twiddles, R = 5 or 7 (the
-// other radices of the butterfly passes use dft<R, S> of spe_fft.cuh):
-// v[q] <- sum_r v[r] exp(S 2 pi i r q / R)
+// The symmetric form of an odd prime DFT (spelled out before any_pass_prime), in
+// place on R registers: (R-1)^2 real multiply-adds instead of the direct
+// sums' 4 (R-1)^2.
 template <int R, int S, int Q, int RR>
-__device__ __forceinline__ void dft_direct_term(const float2* x, float2& acc) {
-  if constexpr (RR < R) {
-    const float2 t = ctwiddle<S, RR * Q, R>(x[RR]);
-    acc = make_float2(acc.x + t.x, acc.y + t.y);
-    dft_direct_term<R, S, Q, RR + 1>(x, acc);
+__device__ __forceinline__ void sym_terms(const float2* a, const float2* b, float2& A, float2& B) {
+  if constexpr (RR <= (R - 1) / 2) {
+    constexpr float c = float(ct_cos_frac(RR * Q, R));
+    constexpr float s = float(S * ct_sin_frac(RR * Q, R));
+    A.x = fmaf(a[RR - 1].x, c, A.x);
+    A.y = fmaf(a[RR - 1].y, c, A.y);
+    B.x = fmaf(b[RR - 1].x, s, B.x);
+    B.y = fmaf(b[RR - 1].y, s, B.y);
+    sym_terms<R, S, Q, RR + 1>(a, b, A, B);
   }
 }
 template <int R, int S, int Q>
-__device__ __forceinline__ void dft_direct_out(const float2* x, float2* v) {
-  if constexpr (Q < R) {
-    float2 acc = x[0];
-    dft_direct_term<R, S, Q, 1>(x, acc);
-    v[Q] = acc;
-    dft_direct_out<R, S, Q + 1>(x, v);
+__device__ __forceinline__ void sym_outputs(const float2* a, const float2* b, float2 x0, float2* v) {
+  if constexpr (Q <= (R - 1) / 2) {
+    float2 A = x0, B = make_float2(0.f, 0.f);
+    sym_terms<R, S, Q, 1>(a, b, A, B);
+    v[Q] = make_float2(A.x - B.y, A.y + B.x);
+    v[R - Q] = make_float2(A.x + B.y, A.y - B.x);
+    sym_outputs<R, S, Q + 1>(a, b, x0, v);
   }
 }
 template <int R, int S>
+__device__ __forceinline__ void dft_odd_sym(float2* v) {
+  constexpr int H = (R - 1) / 2;
+  float2 a[H], b[H];
+  const float2 x0 = v[0];
+  float2 sum = x0;
+#pragma unroll
+  for (int r = 1; r <= H; ++r) {
+    a[r - 1] = cadd(v[r], v[R - r]);
+    b[r - 1] = csub(v[r], v[R - r]);
+    sum = cadd(sum, a[r - 1]);
+  }
+  v[0] = sum;
+  sym_outputs<R, S, 1>(a, b, x0, v);
+}
+
+template <int R, int S>
 __device__ __forceinline__ void small_dft(float2* v) {
   if constexpr (R == 5 || R == 7) {
-    float2 x[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) x[r] = v[r];
-    dft_direct_out<R, S, 0>(x, v);
+    dft_odd_sym<R, S>(v);
   } else {
     dft<R, S>(v);
   }
@@ -134,23 +152,11 @@ __device__ __forceinline__ void any_pass_r(const float2* cur, float2* oth, const
 // multiply-adds for the R outputs, against 4 (R-1)^2 for the direct sums.
 // Output q goes to dst[q * NS] as soon as it is formed, so only the a_r,
 // b_r and one output pair are live.
-template <int R, int S, int Q, int RR>
-__device__ __forceinline__ void odd_sym_terms(const float2* a, const float2* b, float2& A, float2& B) {
-  if constexpr (RR <= (R - 1) / 2) {
-    constexpr float c = float(ct_cos_frac(RR * Q, R));
-    constexpr float s = float(S * ct_sin_frac(RR * Q, R));
-    A.x = fmaf(a[RR - 1].x, c, A.x);
-    A.y = fmaf(a[RR - 1].y, c, A.y);
-    B.x = fmaf(b[RR - 1].x, s, B.x);
-    B.y = fmaf(b[RR - 1].y, s, B.y);
-    odd_sym_terms<R, S, Q, RR + 1>(a, b, A, B);
-  }
-}
 template <int R, int S, int Q>
 __device__ __forceinline__ void odd_sym_outputs(const float2* a, const float2* b, float2 x0, float2* dst, int NS) {
   if constexpr (Q <= (R - 1) / 2) {
     float2 A = x0, B = make_float2(0.f, 0.f);
-    odd_sym_terms<R, S, Q, 1>(a, b, A, B);
+    sym_terms<R, S, Q, 1>(a, b, A, B);
     dst[Q * NS] = make_float2(A.x - B.y, A.y + B.x);
     dst[(R - Q) * NS] = make_float2(A.x + B.y, A.y - B.x);
     odd_sym_outputs<R, S, Q + 1>(a, b, x0, dst, NS);
@@ -355,7 +361,9 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
 }
 
 template <int AXIS, class Op, bool BIG>
-__global__ void __launch_bounds__(BIG ? kAnyThreadsBig : kAnyThreads)
+// BIG kernels: two 256-thread CTAs per SM, 128 registers a thread (a few
+// spilled bytes; one CTA per SM without the cap ran 30% slower at side 1054)
+__global__ void __launch_bounds__(BIG ? kAnyThreadsBig : kAnyThreads, BIG ? 2 : 0)
     pass_any(const Op op, const AnyPlan pl, const float2* __restrict__ tw) {
   constexpr int NT = BIG ? kAnyThreadsBig : kAnyThreads;
   extern __shared__ float2 sm_any[];

@@ -11,9 +11,10 @@ the run-time symmetric pass of primes above 31, 97 (prime) and
 1030 = 2 x 5 x 103 (a detector's side).
 
 Tolerances as for the compiled sides (test_gpu_parity.py): round trip,
-forward transform and projection 2e-6 relative L2, except 5e-6 where a
-pass of a prime radix from 11 sums 5 to 51 products per output; one
-iteration the same; five iterations median 1e-4 (ER 2e-5), each individual
+forward transform and projection 2e-6 relative L2 where every pass has
+radix 2, 3, 4 or 8, 3e-6 with radix-5 / 7 passes and 5e-6 where a pass of a
+prime radix from 11 sums 5 to 51 products per output; one iteration the
+same; five iterations median 1e-4 (ER 2e-5), each individual
 1e-2 (gated ER 3e-2, as at side 2048: phase-gate decisions at the threshold);
 metrics 1e-5 / 1e-4; shrink-wrap supports identical except at pixels within
 1e-4 of the cut.
@@ -29,8 +30,25 @@ pytestmark = pytest.mark.gpu
 SIDES = [1054, 294, 100, 243, 97, 286, 874, 116, 1030]
 
 
+def largest_prime_factor(n):
+    f, p = n, 2
+    best = 1
+    while p * p <= f:
+        while f % p == 0:
+            best, f = p, f // p
+        p += 1
+    return max(best, f) if f > 1 else best
+
+
 def tol1(n):
-    return 5e-6 if n in (1054, 286, 874, 116, 1030) else 2e-6
+    """One transform pair or iteration: 2e-6 where every pass has radix 2, 3,
+    4 or 8; 3e-6 with radix-5 / 7 passes; 5e-6 with a prime of 11 or more
+    (5 to 51 products summed per output).  FP32 emulations of the radix-7
+    butterfly give the same error for its symmetric and direct forms
+    (6.5e-8 / 6.9e-8 relative): the steps are the spread of one iteration,
+    which measures up to 2.3e-6 at 294 = 2 x 3 x 7^2."""
+    p = largest_prime_factor(n)
+    return 2e-6 if p <= 3 else (3e-6 if p <= 7 else 5e-6)
 
 
 def rel(a, b):
