@@ -463,8 +463,8 @@ bool make_plan(int n, AnyPlan& pl) {
   const size_t table = (size_t)n * sizeof(float2);
   const size_t per_line = 2 * (size_t)pl.LS * sizeof(float2);
   if (table + per_line > kAnySmem) return false;
-  // plans with a big prime run 256-thread CTAs, two per SM: half the budget
-  const size_t budget = (pl.big && table + per_line <= kAnySmem / 2) ? kAnySmem / 2 : kAnySmem;
+  // two CTAs per SM where half the budget still holds two lines
+  const size_t budget = (table + 2 * per_line <= kAnySmem / 2) ? kAnySmem / 2 : kAnySmem;
   const size_t w = (budget - table) / per_line;
   pl.W = (int)(w < 8 ? w : 8);
   // the bounds of fdiv: indices below W n < 2^17, divisors below 2^15
