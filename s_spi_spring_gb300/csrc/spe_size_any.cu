@@ -163,15 +163,29 @@ __device__ __forceinline__ void odd_sym_outputs(const float2* a, const float2* b
   }
 }
 
+// The dynamic shared memory of pass_any: two line buffers and the side's
+// twiddle table.  The non-inlined pass functions below take offsets into it
+// (not pointers), so that their accesses are shared-memory accesses, and
+// the plan's values they need by value.
+extern __shared__ float2 sm_any[];
+
+struct PassArgs {  // one pass of the plan, for the non-inlined pass functions
+  int cur, oth, tw;  // offsets of the line buffers and the table in sm_any
+  int nl, n, LS, NS;
+  unsigned inv_m, inv_ns;
+};
+
 // One Stockham pass of an odd prime radix R (11 .. 31) as butterflies: the
 // inputs and twiddles of any_pass_r, the symmetric DFT above.  Not inlined:
 // one copy per (R, S) serves every operation's pass kernel.
 template <int R, int S>
-__device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, const AnyPlan& pl, const float2* tw,
-                                            int nl, int ps) {
+__device__ __noinline__ void any_pass_prime(const PassArgs a) {
   constexpr int H = (R - 1) / 2;
-  const int n = pl.n, LS = pl.LS, m = n / R, NS = pl.ns[ps], tstep = n / (NS * R);
-  const unsigned inv_m = pl.inv_m[ps], inv_ns = pl.inv_ns[ps];
+  const float2* cur = sm_any + a.cur;
+  float2* oth = sm_any + a.oth;
+  const float2* tw = sm_any + a.tw;
+  const int nl = a.nl, n = a.n, LS = a.LS, m = n / R, NS = a.NS, tstep = n / (NS * R);
+  const unsigned inv_m = a.inv_m, inv_ns = a.inv_ns;
   for (int i = threadIdx.x; i < nl * m; i += kAnyThreadsBig) {
     const int c = fdiv(i, inv_m), b = i - c * m;
     const int bq = fdiv(b, inv_ns), k = b - bq * NS;
@@ -217,11 +231,13 @@ __device__ __noinline__ void any_pass_prime(const float2* cur, float2* oth, cons
 // About 2 real multiply-adds per input and output pair instead of 4 per
 // input and output.
 template <int S, int NT>
-__device__ __noinline__ void any_pass_sym(float2* cur, float2* oth, const AnyPlan& pl, const float2* tw, int nl,
-                                          int ps, int R) {
-  const int n = pl.n, LS = pl.LS, NS = pl.ns[ps], H = (R - 1) / 2;
+__device__ __noinline__ void any_pass_sym(const PassArgs a, int R) {
+  float2* cur = sm_any + a.cur;
+  float2* oth = sm_any + a.oth;
+  const float2* tw = sm_any + a.tw;
+  const int nl = a.nl, n = a.n, LS = a.LS, NS = a.NS, H = (R - 1) / 2;
   const int m = n / R, tstep = n / (NS * R);
-  const unsigned inv_m = pl.inv_m[ps], inv_ns = pl.inv_ns[ps];
+  const unsigned inv_m = a.inv_m, inv_ns = a.inv_ns;
   const unsigned inv_h = fdiv_inv(H), inv_h1 = fdiv_inv(H + 1);
   // 1. twiddles and pairs, in place
   for (int i = threadIdx.x; i < nl * m * H; i += NT) {
@@ -338,15 +354,17 @@ __device__ __forceinline__ void fft_any(float2*& cur, float2*& oth, const AnyPla
       case 8: any_pass_r<8, S, NT>(cur, oth, pl, tw, nl, ps); break;
       default:
         if constexpr (BIG) {
+          const PassArgs a{(int)(cur - sm_any), (int)(oth - sm_any), (int)(tw - sm_any), nl, pl.n, pl.LS, pl.ns[ps],
+                           pl.inv_m[ps], pl.inv_ns[ps]};
           switch (R) {
-            case 11: any_pass_prime<11, S>(cur, oth, pl, tw, nl, ps); break;
-            case 13: any_pass_prime<13, S>(cur, oth, pl, tw, nl, ps); break;
-            case 17: any_pass_prime<17, S>(cur, oth, pl, tw, nl, ps); break;
-            case 19: any_pass_prime<19, S>(cur, oth, pl, tw, nl, ps); break;
-            case 23: any_pass_prime<23, S>(cur, oth, pl, tw, nl, ps); break;
-            case 29: any_pass_prime<29, S>(cur, oth, pl, tw, nl, ps); break;
-            case 31: any_pass_prime<31, S>(cur, oth, pl, tw, nl, ps); break;
-            default: any_pass_sym<S, NT>(cur, oth, pl, tw, nl, ps, R); break;
+            case 11: any_pass_prime<11, S>(a); break;
+            case 13: any_pass_prime<13, S>(a); break;
+            case 17: any_pass_prime<17, S>(a); break;
+            case 19: any_pass_prime<19, S>(a); break;
+            case 23: any_pass_prime<23, S>(a); break;
+            case 29: any_pass_prime<29, S>(a); break;
+            case 31: any_pass_prime<31, S>(a); break;
+            default: any_pass_sym<S, NT>(a, R); break;
           }
         }
         // (kernels without BIG never see a radix of 11 or more: make_plan
@@ -366,7 +384,6 @@ template <int AXIS, class Op, bool BIG>
 __global__ void __launch_bounds__(BIG ? kAnyThreadsBig : kAnyThreads, BIG ? 2 : 0)
     pass_any(const Op op, const AnyPlan pl, const float2* __restrict__ tw) {
   constexpr int NT = BIG ? kAnyThreadsBig : kAnyThreads;
-  extern __shared__ float2 sm_any[];
   const int n = pl.n, W = pl.W, LS = pl.LS;
   float2* cur = sm_any;
   float2* oth = sm_any + (size_t)W * LS;
