@@ -46,6 +46,7 @@ B_PER_PIXEL_ITER = 24  # rho read+write 16 B, amplitude 4 B, support 4 B
 ITER_DRAM_BYTES = {
     (8, 104, 0, 1): 757_700_000,   # 135.3 + 78.4 + 335.6 + 208.4 MB, one whole-range lane
     (8, 104, 32, 2): 634_000_000,  # 2 x (68.2 + 8.9 + 167.8 + 72.1) MB, two 32-individual lanes
+    (8, 702, 32, 2): 631_000_000,  # 2 x (68.2 + 8.8 + 167.8 + 70.7) MB, one-stage 2-row tiles, two lanes
 }
 E2E_BLOCKS = 2  # population blocks of the host-buffer call (measured best of 1-16)
 

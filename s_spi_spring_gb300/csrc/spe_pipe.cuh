@@ -28,6 +28,7 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Column exchange layout that keeps the element pairs of a 16-byte copy
 // adjacent (columns are never permuted, only rows).  W = 16: plain rows of
@@ -387,6 +388,93 @@ __global__ void __launch_bounds__(RowCfg<N, W, XLay>::NT, RowCfg<N, W, XLay>::MI
     for (int e = 0; e < E; ++e) T[rowbase + elem_pos<N>(e, j)] = v[e];
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// The row pass with one stage instead of two (tile codes 700 + W): the
+// next tile's rows of T are copied into the stage as soon as this tile's
+// have been read into registers, and its rows of the previous iterate and
+// the support as soon as the update has read this tile's, so the copies
+// still overlap the transforms while the stage takes half the shared
+// memory (at 2048: 73 KB a CTA instead of 113 KB, three CTAs per SM instead
+// of two).  The per-element arithmetic is k_rows_iterate's: bit-identical.
+// ---------------------------------------------------------------------------
+template <int N, int W, class XLay = LayPad<N, W>>
+struct Row1Cfg : RowCfg<N, W, XLay> {
+  using B = RowCfg<N, W, XLay>;
+  static constexpr size_t SMEM = (size_t)B::TWB + B::R_X + B::STAGE;
+};
+
+template <int N, int W, int UPD, class XLay = LayPad<N, W>>
+__global__ void __launch_bounds__(Row1Cfg<N, W, XLay>::NT, Row1Cfg<N, W, XLay>::MINB)
+    k_rows_iterate1(float2* __restrict__ T, float2* __restrict__ rho, const int* __restrict__ S, int first,
+                    int count, float scale, float beta, Gate g, const float2* __restrict__ twg) {
+  using C = Row1Cfg<N, W, XLay>;
+  constexpr int NT = C::NT, E = C::E, TPT = C::TPT, TPI = N / W;
+  using Lay = XLay;
+  extern __shared__ __align__(128) unsigned char sm[];
+  float2* tw = reinterpret_cast<float2*>(sm);
+  float2* xb = reinterpret_cast<float2*>(sm + C::TWB);
+  unsigned char* st = sm + C::TWB + C::R_X;
+  float2* sT = reinterpret_cast<float2*>(st);
+  float2* sR = reinterpret_cast<float2*>(st + C::R_T);
+  int* sS = reinterpret_cast<int*>(st + C::R_T + C::R_R);
+  pdl_enter();
+  load_twiddles<N>(tw, twg, NT);
+  pdl_wait();
+  const int t = threadIdx.x;
+  const int j = t % TPT, c = t / TPT;
+  const int ntiles = count * TPI;
+  constexpr bool NEED_PREV = (UPD != UPD_ER);
+  auto tile_base = [&](int tile) {
+    return (size_t)(first + tile / TPI) * N * N + (size_t)((tile % TPI) * W) * N;
+  };
+  auto stage_T = [&](int tile) {
+    const size_t base = tile_base(tile);
+    for (int q = t; q < N * W / 2; q += NT) cp_async16(&sT[2 * q], T + base + 2 * q);
+  };
+  auto stage_RS = [&](int tile) {
+    const size_t base = tile_base(tile);
+    if (NEED_PREV)
+      for (int q = t; q < N * W / 2; q += NT) cp_async16(&sR[2 * q], rho + base + 2 * q);
+    for (int q = t; q < N * W / 4; q += NT) cp_async16(&sS[4 * q], S + base + 4 * q);
+  };
+
+  int tile = blockIdx.x;
+  if (tile < ntiles) {
+    stage_T(tile);
+    stage_RS(tile);
+  }
+  cp_async_commit();
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int nxt = tile + gridDim.x;
+    cp_async_wait_all();
+    __syncthreads();  // this tile's rows are in the stage
+    const size_t rowbase = tile_base(tile) + (size_t)c * N;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = sT[c * N + elem_pos<N>(e, j)];
+    __syncthreads();  // every thread has read its elements of T
+    if (nxt < ntiles) stage_T(nxt);
+    cp_async_commit();
+    fft_reg<N, Lay, -1>(v, xb, tw, c, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int l = elem_pos<N>(e, j);
+      const float2 rp = __fmul2_rn(v[e], make_float2(scale, scale));
+      const float2 prev = NEED_PREV ? sR[c * N + l] : make_float2(0.f, 0.f);
+      const float2 r = update<UPD>(rp, prev, sS[c * N + l], beta, g);
+      rho[rowbase + l] = r;
+      v[e] = r;
+    }
+    __syncthreads();  // every thread has read its elements of the previous iterate and the support
+    if (nxt < ntiles) stage_RS(nxt);
+    cp_async_commit();
+    fft_reg<N, Lay, +1>(v, xb, tw, c, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) T[rowbase + elem_pos<N>(e, j)] = v[e];
+  }
+  cp_async_wait_all();  // no copy outlives the CTA
 }
 
 // ---------------------------------------------------------------------------

@@ -82,6 +82,12 @@ constexpr bool row_ok() {
   return W <= N && N % W == 0 && RowCfg<N, W, XLay>::NT % 32 == 0 && RowCfg<N, W, XLay>::NT <= 1024 &&
          RowCfg<N, W, XLay>::SMEM <= kMaxSmem;
 }
+// the one-stage row pass (k_rows_iterate1): where the two-stage one fits
+// fewer CTAs per SM than it would
+template <int N, int W>
+constexpr bool row1_ok() {
+  return row_ok<N, W>() && Row1Cfg<N, W>::SMEM <= kMaxSmem;
+}
 // the row pass with per-exchange paddings (LayRowX), where they differ from
 // the plain l + l/16 layout
 template <int N, int W>
@@ -255,6 +261,21 @@ cudaError_t launch_rows_iterate(const Ctx& c, float scale, float beta, Gate g) {
                     scale, beta, g, c.tw);
 }
 
+template <int N, int W, int UPD>
+cudaError_t launch_rows_iterate1(const Ctx& c, float scale, float beta, Gate g) {
+  using P = Row1Cfg<N, W>;
+  auto kern = k_rows_iterate1<N, W, UPD>;
+  static std::atomic<unsigned long long> configured{0ull};
+  static std::atomic<int> resident[64] = {};
+  cudaError_t e = configure(kern, P::SMEM, configured);
+  if (e != cudaSuccess || c.count <= 0) return e;
+  const int tiles = c.count * (N / W);
+  const int slots = share(resident_ctas(kern, P::NT, P::SMEM, resident), c.grid_div);
+  const int grid = tiles < slots ? tiles : slots;
+  return launch_pdl(kern, grid, P::NT, P::SMEM, c.st, c.T, c.rho, static_cast<const int*>(c.S), c.first, c.count,
+                    scale, beta, g, c.tw);
+}
+
 template <int N, int WP>
 cudaError_t launch_cols_pairs_st(const Ctx& c) {
   using P = PairColStCfg<N, WP>;
@@ -376,7 +397,8 @@ cudaError_t launch_cols_w(const Ctx& c, int w) {
 // row-pass variant code: W rows per tile; 100 + W the per-exchange
 // padding; 400 + W row pairs with split real / imaginary parts
 // (spe_pairs.cuh); 500 + W / 600 + W tiles moved by the TMA (spe_tma.cuh)
-// with the plain / the per-exchange padding
+// with the plain / the per-exchange padding; 700 + W one stage instead of
+// two (k_rows_iterate1)
 template <int N, int UPD>
 cudaError_t launch_rows_w(const Ctx& c, int w, float scale, float beta, Gate g) {
   switch (w) {
@@ -394,6 +416,9 @@ cudaError_t launch_rows_w(const Ctx& c, int w, float scale, float beta, Gate g) 
     case 4: if constexpr (row_ok<N, 4>()) return launch_rows_iterate<N, 4, UPD>(c, scale, beta, g); break;
     case 8: if constexpr (row_ok<N, 8>()) return launch_rows_iterate<N, 8, UPD>(c, scale, beta, g); break;
     case 16: if constexpr (row_ok<N, 16>()) return launch_rows_iterate<N, 16, UPD>(c, scale, beta, g); break;
+    case 701: if constexpr (row1_ok<N, 1>()) return launch_rows_iterate1<N, 1, UPD>(c, scale, beta, g); break;
+    case 702: if constexpr (row1_ok<N, 2>()) return launch_rows_iterate1<N, 2, UPD>(c, scale, beta, g); break;
+    case 704: if constexpr (row1_ok<N, 4>()) return launch_rows_iterate1<N, 4, UPD>(c, scale, beta, g); break;
     case 101: if constexpr (xrow_ok<N, 1>()) return launch_rows_iterate<N, 1, UPD, LayRowX<N, 1>>(c, scale, beta, g); break;
     case 102: if constexpr (xrow_ok<N, 2>()) return launch_rows_iterate<N, 2, UPD, LayRowX<N, 2>>(c, scale, beta, g); break;
     case 104: if constexpr (xrow_ok<N, 4>()) return launch_rows_iterate<N, 4, UPD, LayRowX<N, 4>>(c, scale, beta, g); break;
@@ -511,6 +536,9 @@ struct SizeImpl {
     if constexpr (pairrow_ok<N, 1>()) out[k++] = 402;
     if constexpr (pairrow_ok<N, 2>()) out[k++] = 404;
     if constexpr (pairrow_ok<N, 4>()) out[k++] = 408;
+    if constexpr (row1_ok<N, 1>()) out[k++] = 701;
+    if constexpr (row1_ok<N, 2>()) out[k++] = 702;
+    if constexpr (row1_ok<N, 4>()) out[k++] = 704;
     if constexpr (row_ok<N, 1>()) out[k++] = 1;
     if constexpr (row_ok<N, 2>()) out[k++] = 2;
     if constexpr (row_ok<N, 4>()) out[k++] = 4;

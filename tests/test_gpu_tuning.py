@@ -3,7 +3,8 @@
 Every compiled tile width -- including the column pass that keeps two
 columns per thread (negative widths), the one with a warp per column
 (100 + width) and the paired-line passes with split real and imaginary parts
-(400 + width, and 500 + width with register prefetch) -- performs the same
+(400 + width), the TMA row passes (500 / 600 + width) and the one-stage row
+pass (700 + width) -- performs the same
 per-element arithmetic, so all variants must give bit-identical results; the
 autotuner must leave the population as it found it."""
 import itertools
@@ -34,7 +35,7 @@ def test_all_tile_widths_bit_identical(n):
     tried = 0
     for wc, wr in itertools.product([4, 8, 16, -4, -8, -16, 104, 108, 116, 204, 208, 304, 308, 608, 616],
                                     [1, 2, 4, 8, 16, 101, 102, 104, 108, 402, 404, 408, 502, 504, 508, 602, 604,
-                                     608]):
+                                     608, 701, 702, 704]):
         try:
             e.set_tiles(wc, wr)
         except _lib.EngineError:
@@ -49,6 +50,36 @@ def test_all_tile_widths_bit_identical(n):
     assert tried >= 2
     with pytest.raises(_lib.EngineError):
         e.set_tiles(3, 0)
+
+
+@pytest.mark.parametrize("n", [256, 512, 1024, 2048])
+def test_one_stage_row_pass_bit_identical_for_every_update(n):
+    """The one-stage row pass (tile codes 700 + W) against the two-stage one
+    (W) for HIO, RAAR and ER with the reality gate: the ER update reads no
+    previous iterate, the others do."""
+    P = 3
+    e, dens, S = engine(n, P, seed=7)
+    for w in (1, 2, 4):
+        out = []
+        for code in (w, 700 + w):
+            try:
+                e.set_tiles(8 if n <= 1024 else 4, code)
+            except _lib.EngineError:
+                break
+            res = []
+            for alg in ("hio", "raar", "er"):
+                e.upload(0, dens, S)
+                if alg == "hio":
+                    e.hio(0, P, 3, 0.9, 0.0)
+                elif alg == "raar":
+                    e.raar(0, P, 3, 0.87, 0.0)
+                else:
+                    e.er(0, P, 3, 0.5)
+                res.append(e.download(0, P)[0])
+            out.append(res)
+        if len(out) == 2:
+            for a, b in zip(*out):
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (n, w)
 
 
 def test_autotune_restores_population_and_picks_compiled_widths():
