@@ -708,18 +708,34 @@ def run_engine(args):
         _lib.call("spe_iterate_host", eng.h, 0, POP, fp(h_dens), ip(h_supp), _lib.SPE_OP_RAAR, args.iters, BETA,
                   0.0, fp(h_out), E2E_BLOCKS)
 
+    e2e_steps = {}
+
     def e2e_time(step):
         for _ in range(max(1, args.warmup)):
             step()
         barrier()
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        ev[0].record(stream)
+        for k in range(args.steps):
             step()
+            ev[k + 1].record(stream)
+        ev[-1].synchronize()
+        e2e_steps[step.__name__] = [round(ev[k].elapsed_time(ev[k + 1]), 2) for k in range(args.steps)]
+        return max_over_ranks(ev[0].elapsed_time(ev[-1]) / args.steps, world, f"cuda:{local}")
+
+    def copy_gbps():
+        """Host-device bandwidth of the step's copies (one upload, one download)."""
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        _lib.call("spe_upload", eng.h, 0, POP, fp(h_dens), ip(h_supp))
         e1.record(stream)
-        e1.synchronize()
-        return max_over_ranks(e0.elapsed_time(e1) / args.steps, world, f"cuda:{local}")
+        _lib.call("spe_download", eng.h, 0, POP, fp(h_out), None)
+        e2.record(stream)
+        e2.synchronize()
+        h2d = (h_dens.numel() + h_supp.numel()) * 4 / (e0.elapsed_time(e1) / 1e3) / 1e9
+        d2h = h_out.numel() * 4 / (e1.elapsed_time(e2) / 1e3) / 1e9
+        return round(h2d, 1), round(d2h, 1)
 
     key = (tiles[0], tiles[1], sched[0], sched[1])
     traffic = ITER_DRAM_BYTES.get(key)
@@ -728,13 +744,15 @@ def run_engine(args):
                       if traffic else f"no ncu capture of tiles {tiles[0]},{tiles[1]} / schedule "
                                       f"{sched[0]},{sched[1]}")
 
-    # e2e: upload, RAAR and download as three C-ABI calls per step (the
-    # engine's tuned two-lane schedule inside the RAAR call); the one-call
-    # host-buffer interface with its copies overlapping the other block's
-    # iterations is reported beside it (its lanes' relative phase follows the
-    # copies, and measured 275k-336k over runs against 333.8k-333.9k here)
-    e2e_value = units_per_step * world / (e2e_time(e2e_serial) / 1e3)
-    e2e_pipelined_value = units_per_step * world / (e2e_time(e2e_pipelined) / 1e3)
+    # e2e: the one-call host-buffer interface (Solver::RAAR's shape: host
+    # densities in and out, one block's download overlapping the other
+    # block's iterations); the three-call sequence upload / RAAR / download
+    # is reported beside it, with the per-step times of both and the copy
+    # bandwidth before and after (single slow steps were seen in both)
+    gbps_before = copy_gbps()
+    e2e_serial_value = units_per_step * world / (e2e_time(e2e_serial) / 1e3)
+    e2e_value = units_per_step * world / (e2e_time(e2e_pipelined) / 1e3)
+    gbps_after = copy_gbps()
 
     out = {
         "metric": "iter*individuals/s (RAAR, 512^2, population 64)",
@@ -755,9 +773,10 @@ def run_engine(args):
         "e2e": {"value": round(e2e_value, 1), "unit": "iter*individuals/s",
                 "h2d_bytes_per_step": int(h_dens.numel() * 4 + h_supp.numel() * 4),
                 "d2h_bytes_per_step": int(h_out.numel() * 4),
-                "call": "spe_upload + spe_raar + spe_download (pinned host buffers)",
-                "iterate_host_pipelined": round(e2e_pipelined_value, 1),
-                "iterate_host_call": f"spe_iterate_host ({E2E_BLOCKS} blocks on two streams)"},
+                "call": f"spe_iterate_host (pinned host buffers, {E2E_BLOCKS} blocks on two streams)",
+                "upload_raar_download": round(e2e_serial_value, 1),
+                "ms_per_step": e2e_steps,
+                "copy_gbps_h2d_d2h": [gbps_before, gbps_after]},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "traffic_source": traffic_source,
