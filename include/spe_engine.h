@@ -397,8 +397,8 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
  * (SPE_ERR_UNSUPPORTED); host only, no device needed.  compiled (may be
  * NULL) receives 1 for the sides with a compiled register-resident plan
  * (16, 32, 64, 128, 256, 384, 512, 768, 1024, 2048) and 0 for the sides the
- * any-side kernels run (every other side whose prime factors are at most
- * 257 and whose lines fit in shared memory, n <= 14079).  The reference
+ * any-side kernels run (every other side from 2 whose lines fit in shared
+ * memory, n <= 9386, whatever its prime factors).  The reference
  * accepts every side (cufftPlan2d, src/gpu/gpu_context.h:29); this query has
  * no counterpart there. */
 int spe_side_supported(int n, int* compiled);

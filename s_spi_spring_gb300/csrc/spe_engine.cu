@@ -428,8 +428,8 @@ int spe_side_supported(int n, int* compiled) {
   if (compiled) *compiled = 0;
   const spe::SizeOps* ops = n > 0 ? spe::size_ops(n) : nullptr;
   if (!ops)
-    return fail(SPE_ERR_UNSUPPORTED, "pattern side %d is not supported: a side needs prime factors of at most 257 "
-                "and at most 14079 pixels", n);
+    return fail(SPE_ERR_UNSUPPORTED, "pattern side %d is not supported: a side needs at least 2 and at most 9386 "
+                "pixels (its lines are held in shared memory)", n);
   if (compiled) *compiled = spe::size_ops_any(n) != ops;
   return SPE_OK;
 }
@@ -475,8 +475,8 @@ int spe_create(int n, int device, spe_engine** out) {
   const spe::SizeOps* ops = spe::size_ops(n);
   if (!ops)
     return fail(SPE_ERR_UNSUPPORTED,
-                "pattern side %d is not supported: a side needs prime factors of at most 257 and at most 14079 "
-                "pixels (sides 16,32,64,128,256,384,512,768,1024,2048 run compiled plans)", n);
+                "pattern side %d is not supported: a side needs at least 2 and at most 9386 pixels (sides "
+                "16,32,64,128,256,384,512,768,1024,2048 run compiled plans)", n);
   int ndev = 0;
   CK(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
   if (device < 0 || device >= ndev) return fail(SPE_ERR_INVALID, "device %d not present (%d devices)", device, ndev);

@@ -19,9 +19,9 @@
 // butterflies in registers (a thread reads the R inputs of one butterfly,
 // applies its twiddles and the radix-R DFT, writes R outputs), and so do the
 // primes 11 .. 31, with the symmetric form of the prime DFT; a larger prime
-// radix runs the same symmetric form with run-time R over shared memory
-// (about R real multiply-adds per point): sides whose largest prime factor
-// exceeds kMaxPrime are rejected rather than run at that cost.
+// radix, up to the side itself, runs the same symmetric form with run-time
+// R over shared memory (about R real multiply-adds per point).  Sides are
+// limited only by their lines fitting in shared memory (n <= 9386).
 #include <map>
 #include <memory>
 #include <mutex>
@@ -33,7 +33,6 @@ namespace {
 
 constexpr int kAnyThreads = 512;     // threads of a pass CTA
 constexpr int kAnyThreadsBig = 256;  // the same for plans with a prime radix of 11 or more (128 registers each)
-constexpr int kMaxPrime = 257;       // largest prime factor accepted
 constexpr int kMaxRadices = 24;
 constexpr size_t kAnySmem = 220 * 1024;  // shared-memory budget of one CTA (two line buffers)
 
@@ -55,7 +54,7 @@ struct AnyPlan {
 // x / d as one multiply-high, inv = ceil(2^32 / d) (0 encodes d = 1).  Exact
 // for x < 2^17 and d < 2^15: with x = q d + s and inv d = 2^32 + r, r < d,
 // x inv / 2^32 = q + (s + x r / 2^32) / d, and s + x r / 2^32 < d.  Every
-// index divided here is below W n <= 8 * 14079 < 2^17 (make_plan checks).
+// index divided here is below W n <= 8 * 9386 < 2^17 (make_plan checks).
 __host__ __device__ constexpr unsigned fdiv_inv(int d) { return d <= 1 ? 0u : 0xFFFFFFFFu / (unsigned)d + 1u; }
 __device__ __forceinline__ int fdiv(int x, unsigned inv) { return inv ? (int)__umulhi((unsigned)x, inv) : x; }
 
@@ -459,7 +458,6 @@ bool make_plan(int n, AnyPlan& pl) {
   }
   for (int f = 2; f <= m && pl.nrad < kMaxRadices;) {
     if (m % f == 0) {
-      if (f > kMaxPrime) return false;
       pl.rad[pl.nrad++] = f;
       m /= f;
     } else {

@@ -35,14 +35,23 @@ def test_version(lib):
     assert lib.spe_version() >= 100
 
 
-@pytest.mark.parametrize("n", [263, 2 * 7919, 14336])
+@pytest.mark.parametrize("n", [1, 9387, 2 * 7919, 14336])
 def test_unsupported_size_fails_loudly(n):
-    """Sides with a prime factor above 257 (263, 2 x 7919) or lines too long
-    for shared memory (14336 = 2^11 x 7) are rejected before any device call;
-    every other side runs (compiled plans or the any-side kernels)."""
+    """Sides whose lines are too long for shared memory (from 9387; 2 x 7919,
+    14336 = 2^11 x 7) and side 1 are rejected before any device call; every
+    other side runs (compiled plans or the any-side kernels)."""
     with pytest.raises(_lib.EngineError) as ei:
         _lib.Engine(n, 0)
     assert ei.value.code == 4  # SPE_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("n,compiled", [(512, True), (2048, True), (1054, False), (263, False), (1031, False),
+                                        (2 * 263, False), (9386, False)])
+def test_side_supported_any_prime_factor(n, compiled):
+    """Host-only query: compiled plans, and every other side up to 9386
+    (two line buffers and the side's table in 220 KB of shared memory)
+    whatever its prime factors (263 and 1031 are primes)."""
+    assert _lib.side_supported(n) == ("compiled" if compiled else "any")
 
 
 def _patterns():

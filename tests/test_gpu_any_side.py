@@ -7,8 +7,8 @@ to max(shape) (spring/pattern_manager.py:61-66), so the reference's own
 1054 x 1024 example patterns run at 1054 = 2 x 17 x 31.  Sides here: 1054;
 294 = 2 x 3 x 7^2; 100 = 4 x 5^2; 243 = 3^5; for the symmetric prime
 butterflies 286 = 2 x 11 x 13, 874 = 2 x 19 x 23 and 116 = 4 x 29; and for
-the run-time symmetric pass of primes above 31, 97 (prime) and
-1030 = 2 x 5 x 103 (a detector's side).
+the run-time symmetric pass of primes above 31, 97 (prime),
+1030 = 2 x 5 x 103 (a detector's side) and 526 = 2 x 263.
 
 Tolerances as for the compiled sides (test_gpu_parity.py): round trip,
 forward transform and projection 2e-6 relative L2 where every pass has
@@ -27,7 +27,7 @@ from s_spi_spring_gb300 import _lib, synthetic
 
 pytestmark = pytest.mark.gpu
 
-SIDES = [1054, 294, 100, 243, 97, 286, 874, 116, 1030]
+SIDES = [1054, 294, 100, 243, 97, 286, 874, 116, 1030, 526]
 
 
 def largest_prime_factor(n):
