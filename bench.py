@@ -47,6 +47,10 @@ ITER_DRAM_BYTES = {
     (8, 104, 0, 1): 757_700_000,   # 135.3 + 78.4 + 335.6 + 208.4 MB, one whole-range lane
     (8, 104, 32, 2): 634_000_000,  # 2 x (68.2 + 8.9 + 167.8 + 72.1) MB, two 32-individual lanes
     (8, 702, 32, 2): 631_000_000,  # 2 x (68.2 + 8.8 + 167.8 + 70.7) MB, one-stage 2-row tiles, two lanes
+    (8, 701, 32, 2): 631_700_000,  # 2 x (68.2 + 8.8 + 167.8 + 71.0) MB, one-stage 1-row tiles
+    (8, 704, 32, 2): 632_100_000,  # 2 x (68.2 + 8.8 + 167.8 + 71.2) MB, one-stage 4-row tiles
+    (8, 102, 32, 2): 631_400_000,  # 2 x (68.2 + 8.8 + 167.8 + 70.9) MB, 2-row tiles, per-exchange padding
+    (8, 4, 32, 2): 633_300_000,    # 2 x (68.2 + 8.8 + 167.8 + 71.8) MB, 4-row tiles, plain padding
 }
 E2E_BLOCKS = 2  # population blocks of the host-buffer call (measured best of 1-16)
 
