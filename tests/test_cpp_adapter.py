@@ -7,7 +7,7 @@ include/spe_engine.h, and linked to the in-tree engine library.
 Compiling it checks, through static_asserts in engine_solver.cpp, that every
 EngineSolver method has exactly the signature of the reference's Solver
 method it replaces and that the reference's element types are the engine's.
-The driver then builds the reference's Reconstruction objects, hands them to
+The test program then builds the reference's Reconstruction objects, hands them to
 the seam, and -- without a GPU here -- checks that constructing the solver
 reports the missing device as an exception carrying the engine's message
 instead of crashing.  Needs the reference checkout: skipped without it (the
