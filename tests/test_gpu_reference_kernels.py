@@ -93,6 +93,30 @@ def test_engine_matches_reference_kernels(n, alg, beta, real):
     e.close()
 
 
+@pytest.mark.parametrize("n,tol", [(1024, 5e-6), (2048, 5e-6), (1054, 1e-5)])
+@pytest.mark.parametrize("alg,beta,real", ALGS)
+def test_engine_matches_reference_kernels_large_and_any_sides(n, tol, alg, beta, real):
+    """One iteration against the reference's kernels with cuFFT at the
+    larger compiled sides and at 1054 = 2 x 17 x 31 (the reference's example
+    patterns; the engine's run-time kernels against cuFFT's plan for that
+    side): 5e-6 relative at the compiled sides as at the smaller ones, 1e-5
+    at 1054, where each float32 path lies within 5e-6 of float64."""
+    A, dens, S = case(n, 2, n + 13)
+    r = ref_gpu.RefGPU(n, A)
+    want = r.iterate(dens, S, alg, 1, beta, real)
+    r.close()
+    e = _lib.Engine(n, 0)
+    e.set_amplitudes(A)
+    e.upload(0, dens, S)
+    {"HIO": lambda: e.hio(0, 2, 1, beta, real), "RAAR": lambda: e.raar(0, 2, 1, beta, real),
+     "ER": lambda: e.er(0, 2, 1, real)}[alg]()
+    got, _ = e.download(0, 2)
+    e.close()
+    rels = [rel(got[i], want[i]) for i in range(2)]
+    print(alg, n, rels)
+    assert max(rels) < tol, (alg, n, rels)
+
+
 def test_final_rfactor_matches_reference_kernels():
     n, P = 512, 8
     A, dens, S = case(n, P, 7)
