@@ -174,7 +174,7 @@ def object_like(n, count, seed):
     return A, cur, S, e
 
 
-@pytest.mark.parametrize("n", [64, 256, 512])
+@pytest.mark.parametrize("n", [64, 256, 512, 1054, 2048])
 @pytest.mark.parametrize("reality", [0.0, 0.5])
 def test_evaluate_matches_reference_kernels(n, reality):
     A, cur, S, e = object_like(n, 3, n + 5)
@@ -200,7 +200,7 @@ def cut_agrees(got, want, m, cut):
     return int(diff.sum()), bool(np.all(near[diff]))
 
 
-@pytest.mark.parametrize("n", [64, 256, 512])
+@pytest.mark.parametrize("n", [64, 256, 512, 1054, 2048])
 def test_shrinkwrap_matches_reference_kernels(n):
     A, cur, S, e = object_like(n, 2, n + 7)
     r = ref_gpu.RefGPU(n, A)
