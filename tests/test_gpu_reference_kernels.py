@@ -247,7 +247,8 @@ def shifted_copies(n, P, seed):
     return A, np.stack(rhos), np.stack(Ss)
 
 
-@pytest.mark.parametrize("n,minr,maxr", [(128, 0.0, 2.0), (256, 0.0, 2.0), (256, 0.05, 0.8)])
+@pytest.mark.parametrize("n,minr,maxr", [(128, 0.0, 2.0), (256, 0.0, 2.0), (256, 0.05, 0.8), (1054, 0.0, 2.0),
+                                         (2048, 0.05, 0.8)])
 def test_reshift_matches_reference_kernels(n, minr, maxr):
     P = 6
     A, rhos, Ss = shifted_copies(n, P, seed=n + 1)
@@ -270,10 +271,11 @@ def test_reshift_matches_reference_kernels(n, minr, maxr):
         assert d < 1e-5, (i, d)
 
 
-@pytest.mark.parametrize("crossft,use_average,update_support,seed",
-                         [(1.0, 0.0, True, 17), (0.0, 0.0, True, 18), (0.5, 0.5, False, 19), (1.0, -0.5, True, 20)])
-def test_crossover_matches_reference_kernels(crossft, use_average, update_support, seed):
-    n, P = 128, 6
+@pytest.mark.parametrize("n,crossft,use_average,update_support,seed",
+                         [(128, 1.0, 0.0, True, 17), (128, 0.0, 0.0, True, 18), (128, 0.5, 0.5, False, 19),
+                          (128, 1.0, -0.5, True, 20), (1054, 0.5, 0.5, True, 21)])
+def test_crossover_matches_reference_kernels(n, crossft, use_average, update_support, seed):
+    P = 6
     A, rhos, Ss = shifted_copies(n, P, seed=seed)
     errors = np.random.default_rng(seed).uniform(0.1, 0.9, P).astype(np.float32)
     best = int(np.argmin(errors))
