@@ -36,7 +36,7 @@ def kernel_loss_grad(eng, dens, S, loss, eps, weights=None):
     return L.detach().cpu().numpy(), d.grad.cpu().numpy()
 
 
-@pytest.mark.parametrize("n", [64, 128, 512])
+@pytest.mark.parametrize("n", [64, 128, 512, 1024, 1054])
 @pytest.mark.parametrize("loss,eps", [("amplitude", 0.0), ("poisson", 1e-3)])
 def test_loss_and_gradient_match_fp64_oracle(n, loss, eps):
     P = 3
