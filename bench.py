@@ -346,29 +346,41 @@ def memetic(args, local, tiles, sched):
     I, _, _ = synthetic.polygon_pattern(seed=1, n=N, diameter=120.0, photons=1e7, stop_radius=8, gap=4, stripes=2)
     st = MemeticSettings(generations=10, popsize=POP, alg="RAAR", it=args.iters, beta=BETA, it_ER=20, it_eval=20,
                          sigma=3.0, threshold=0.1)
-    sol = Solver(I, gpus=[local], seed=42)
-    sol.engine.set_tiles(*tiles)
-    sol.engine.set_schedule(*sched)
-    recs = sol.InitializePop(POP, 128, itemsize=[128 * 0.2, 128 * 0.9], nitems=[2, 8], exponent=[0.5, 0.5],
-                             scaling=[0.5, 1.5], phaserange=0)
-    run = MemeticRun(sol, recs, st)
-    run.start()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    iters = 0
-    for _ in range(args.memetic_gens):
-        seq = run.algman.sequence(run.generation + 1, area=[1, 1])
-        per_pop = sum(int(p[0]) for name, p in seq if name in ("HIO", "RAAR", "ER"))
-        iters += 2 * POP * per_pop  # parents and children
-        run.step()
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
+
+    def timed(merge):
+        st.merge_sequences = merge
+        sol = Solver(I, gpus=[local], seed=42)
+        sol.engine.set_tiles(*tiles)
+        sol.engine.set_schedule(*sched)
+        recs = sol.InitializePop(POP, 128, itemsize=[128 * 0.2, 128 * 0.9], nitems=[2, 8], exponent=[0.5, 0.5],
+                                 scaling=[0.5, 1.5], phaserange=0)
+        run = MemeticRun(sol, recs, st)
+        run.start()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        iters = 0
+        for _ in range(args.memetic_gens):
+            seq = run.algman.sequence(run.generation + 1, area=[1, 1])
+            per_pop = sum(int(p[0]) for name, p in seq if name in ("HIO", "RAAR", "ER"))
+            iters += 2 * POP * per_pop  # parents and children
+            run.step()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        return dt, iters, run
+
+    dt, iters, run = timed(False)
+    dt_m, _, run_m = timed(True)
+    same = [h["best"] for h in run.history] == [h["best"] for h in run_m.history]
     return {"generations": args.memetic_gens, "s_per_generation": round(dt / args.memetic_gens, 4),
             "iter_ind_per_s": round(iters / dt, 1), "best_error": [round(h["best"], 6) for h in run.history],
             "replaced": [h["replaced"] for h in run.history],
             "what": "MPR generation (SW, Reshift, GetAverage, Crossover, Sequence x2, replacement) through the "
                     "Solver front end, individuals resident on the device; iterations counted over HIO/RAAR/ER "
-                    "ops of both sequences"}
+                    "ops of both sequences",
+            "merged_sequences": {"s_per_generation": round(dt_m / args.memetic_gens, 4),
+                                 "iter_ind_per_s": round(iters / dt_m, 1), "same_history": same,
+                                 "what": "the same loop with the parents' and children's sequences as one engine "
+                                         "call over both lists (bit-identical populations)"}}
 
 
 def batched_sizes(args, local):

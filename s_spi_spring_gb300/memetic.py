@@ -173,6 +173,12 @@ class MemeticSettings:
     refine_steps: int = 0
     refine_lr: float = 1e-3
     refine_loss: str = "poisson"
+    # run the generation's two sequences (parents, then children; the same
+    # op list on independent individuals) as one engine call over both
+    # lists (no reference counterpart; the same populations bit for bit,
+    # fewer calls and a population twice the size per launch).  Off, the
+    # loop makes exactly the reference loop's engine calls.
+    merge_sequences: bool = False
 
     def schedule(self) -> AlgorithmSchedule:
         """``MPR.InitIA`` (``mpr.py:110-140``)."""
@@ -292,8 +298,12 @@ class MemeticRun:
         new = sol.Crossover(self.recs, self.best, self.avg, s.crossprob, s.crossweight, s.crossexp, s.crossft,
                             s.crosssym, s.crossaverage, update_support=not s.refine)
         sol.set_sequence(self.algman.sequence(self.generation, area=suppix, update_support=not s.refine))
-        self.recs = sol.Sequence(self.recs)
-        new = sol.Sequence(new)
+        if s.merge_sequences:
+            both = sol.Sequence(self.recs + new)
+            self.recs, new = both[:len(self.recs)], both[len(self.recs):]
+        else:
+            self.recs = sol.Sequence(self.recs)
+            new = sol.Sequence(new)
         if s.refine_steps > 0:
             self.recs = sol.Refine(self.recs, s.refine_steps, s.refine_lr, s.refine_loss)
             new = sol.Refine(new, s.refine_steps, s.refine_lr, s.refine_loss)

@@ -65,6 +65,19 @@ def test_resident_loop_equals_host_round_trips():
         assert np.array_equal(ra.get_support(), rb.get_support())
 
 
+def test_merged_sequences_equal_the_reference_call_structure():
+    """The parents' and the children's sequences run as one engine call
+    (merge_sequences) give the populations and statistics of the loop that
+    calls them one after the other, as the reference's loop does."""
+    a = run(generations=3)
+    b = run(generations=3, merge_sequences=True)
+    assert [x["best"] for x in a.history] == [x["best"] for x in b.history]
+    assert [x["replaced"] for x in a.history] == [x["replaced"] for x in b.history]
+    for ra, rb in zip(a.recs, b.recs):
+        assert np.array_equal(ra.get_density().view(np.uint32), rb.get_density().view(np.uint32))
+        assert np.array_equal(ra.get_support(), rb.get_support())
+
+
 def test_hio_loop_with_stabilisation_and_sw_first():
     r = run(alg="HIO", beta=0.9, it_stab=3, sw_first=True, generations=2, repetitions=4)
     assert np.isfinite(r.history[-1]["best"])
