@@ -439,6 +439,16 @@ int spe_device_info(int device, char* name, int name_len, char* pci_bus_id, int 
 int spe_iterate_noalloc(int n, void* density, const int32_t* support, const float* amplitudes, int count,
                         int algorithm, int iterations, float beta, float reality, void* cuda_stream);
 
+/* Self-test of the device-side failure reporting (no reference
+ * counterpart).  Queues on the engine's stream one small kernel that waits
+ * on a barrier for a transfer that is never issued, as the TMA row pass
+ * waits for its tile copies; the wait gives up after its bounded number of
+ * polls (about a second), sets the engine's device flag and the kernel
+ * returns.  The next spe_synchronize (or spe_download) then reports
+ * SPE_ERR_CUDA with the timeout message and clears the flag; the context
+ * and the engine stay usable. */
+int spe_selftest_bounded_wait(spe_engine* e);
+
 /* Waits for all work queued on the engine's stream. */
 int spe_synchronize(spe_engine* e);
 

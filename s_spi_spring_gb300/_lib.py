@@ -85,6 +85,7 @@ SIGNATURES = {
     "spe_far_field": (_i, [_vp, _i, _i, _fp]),
     "spe_loss_grad": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp, _vp]),
     "spe_loss_grad_cols": (_i, [_vp, _vp, _vp, _i, _i, _f, _vp, _vp]),
+    "spe_selftest_bounded_wait": (_i, [_vp]),
     "spe_grad_rows": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "spe_set_amplitudes_batch": (_i, [_vp, _fp, _i, _i]),
     "spe_adam_step": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _f, _f, _f, _f, _i, _vp]),
@@ -391,6 +392,10 @@ class Engine:
         """Far-field loss / gradient on device arrays given by address."""
         call("spe_loss_grad", self.h, _vp(density_ptr), _vp(support_ptr), int(count), int(loss), float(eps),
              _vp(loss_ptr or 0), _vp(grad_ptr or 0), _vp(scale_ptr or 0))
+
+    def selftest_bounded_wait(self):
+        """Queues the bounded-wait self-test; the next synchronize reports it."""
+        call("spe_selftest_bounded_wait", self.h)
 
     def loss_grad_cols(self, density_ptr, support_ptr, count, half_ptr, loss=0, eps=0.0, loss_ptr=0):
         """Loss and the adjoint up to its column pass, kept in ``half``."""

@@ -689,6 +689,14 @@ int spe_download(spe_engine* e, int first, int count, float* density, int32_t* s
   return check_device_flag(e);
 }
 
+int spe_selftest_bounded_wait(spe_engine* e) {
+  if (!e) return fail(SPE_ERR_INVALID, "null engine");
+  if (!e->dev_err) return fail(SPE_ERR_INVALID, "the engine has no device flag");
+  CK(cudaSetDevice(e->dev), "cudaSetDevice");
+  CK(spe::launch_wait_selftest(e->dev_err, e->st), "self-test kernel");
+  return SPE_OK;
+}
+
 int spe_device_buffers(spe_engine* e, void** density, void** support) {
   if (!e) return fail(SPE_ERR_INVALID, "null engine");
   if (density) *density = e->rho;

@@ -71,6 +71,9 @@ struct Ctx {
 // side n; false when the side has no TMA row pass or the driver lacks
 // cuTensorMapEncodeTiled.
 size_t row_maps_bytes();
+// the self-test kernel of the bounded waits (spe_tma.cuh): sets *err after
+// its wait gives up
+cudaError_t launch_wait_selftest(int* err, cudaStream_t st);
 bool build_row_maps(void* out, int n, int cap, const float2* T, const float2* rho, const int* S);
 
 // Phase gate (see phase_out in spe_kernels.cuh): float thresholds of

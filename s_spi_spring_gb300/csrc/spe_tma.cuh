@@ -15,8 +15,9 @@
 // Stage layout per array: [N / QX][W][QX].
 //
 // Waits are bounded: a wait that has not completed after kWaitLimit polls
-// sets *err and the CTA leaves the loop (all threads together, by a
-// block-wide vote), after a second bounded wait for its copies in flight.
+// or one second sets *err and the CTA leaves the loop (all threads
+// together, by a block-wide vote), after a second bounded wait for its
+// copies in flight.
 #pragma once
 #include <cuda.h>
 
@@ -24,7 +25,8 @@
 
 namespace spe {
 
-constexpr unsigned kWaitLimit = 1u << 24;
+constexpr unsigned kWaitLimit = 1u << 24;          // polls of one bounded wait
+constexpr unsigned long long kWaitNs = 1000000000ull;  // and its wall-time limit (1 s)
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -46,10 +48,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// polls up to kWaitLimit times; false if the phase did not complete
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// polls until the phase completes, at most kWaitLimit times and for at most
+// kWaitNs of wall time (a try_wait may suspend the thread for a
+// system-dependent time, so the poll count alone does not bound the time);
+// false if the phase did not complete.  The timer is read only after a
+// first failed poll, then every 256 polls.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-  for (unsigned i = 0; i < kWaitLimit; ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (unsigned i = 1; i < kWaitLimit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 0 && global_ns() - t0 > kWaitNs) return false;
+  }
   return false;
 }
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {

@@ -42,6 +42,28 @@ bool encode(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap* m, const void* ba
 
 size_t row_maps_bytes() { return 4 * sizeof(RowMaps); }
 
+// Self-test of the bounded wait and the device flag (spe_selftest_bounded_wait):
+// one CTA arms its mbarrier for 16 bytes that no copy delivers, so the phase
+// never completes; the bounded wait gives up after kWaitLimit polls or kWaitNs
+// of wall time, whichever comes first, and the CTA
+// sets *err and leaves.  No copy is in flight, so nothing outlives the CTA.
+__global__ void __launch_bounds__(32) k_wait_selftest(int* __restrict__ err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_expect_tx(&bar, 16);
+  }
+  __syncthreads();
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+cudaError_t launch_wait_selftest(int* err, cudaStream_t st) {
+  k_wait_selftest<<<1, 32, 0, st>>>(err);
+  return cudaGetLastError();
+}
+
 bool build_row_maps(void* out, int n, int cap, const float2* T, const float2* rho, const int* S) {
   if (!(n == 256 || n == 512 || n == 1024) || cap <= 0) return false;
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();

@@ -88,3 +88,31 @@ def test_swa_clamps_the_pixel_count():
     _, s1 = e.download(0, 3)
     assert np.all(s1 == 1)
     e.close()
+
+
+def test_bounded_wait_timeout_is_reported_once_and_the_engine_stays_usable():
+    """A device-side wait made to run out on purpose, with no fault: the
+    self-test kernel waits on a barrier for a transfer that is never issued
+    (the TMA row pass's bounded wait), gives up after its limit (about a
+    second) and sets the engine's device flag.  The next synchronize reports
+    SPE_ERR_CUDA with the timeout message and clears the flag; the one after
+    succeeds, and an iteration runs and gives the same result as before."""
+    import time
+
+    e, dens, S = engine(n=128, P=2, seed=9)
+    e.raar(0, 2, 3, 0.87)
+    before, _ = e.download(0, 2)
+    e.upload(0, dens, S)
+    t0 = time.perf_counter()
+    e.selftest_bounded_wait()
+    with pytest.raises(_lib.EngineError) as ei:
+        e.synchronize()
+    waited = time.perf_counter() - t0
+    print("bounded wait gave up after", round(waited, 3), "s:", ei.value)
+    assert ei.value.code == 2 and "timed out" in str(ei.value)  # SPE_ERR_CUDA
+    assert waited < 30.0
+    e.synchronize()  # the flag was cleared
+    e.raar(0, 2, 3, 0.87)
+    after, _ = e.download(0, 2)
+    assert np.array_equal(after.view(np.uint32), before.view(np.uint32))
+    e.close()
