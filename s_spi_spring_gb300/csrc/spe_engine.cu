@@ -1154,19 +1154,20 @@ int spe_autotune(spe_engine* e, int first, int count, int iterations, int* cols,
       }
     }
   best_r = whole_r;
-  // a blocked schedule must win by 2%; when the short trials put the two
-  // within 5% of each other, both are timed again over three times the
-  // iterations before deciding
+  // when the short trials put the two within 5% of each other, both are
+  // timed again over ten times the iterations (the gain of a blocked
+  // schedule is a few percent, the size of the short trials' spread); the
+  // blocked one must then win by 1%
   if (!rc && blocked < 1e29f) {
     if (blocked < whole * 1.05f && whole < blocked * 1.05f) {
       float tw = 0.f, tb = 0.f;
-      const int it3 = iterations;
-      iterations = 3 * it3;
+      const int it1 = iterations;
+      iterations = 10 * it1;
       if (!(rc = trial_s(best_c, whole_r, 0, 1, &tw))) rc = trial_s(best_c, blk_r, blk_chunk, blk_lanes, &tb);
-      iterations = it3;
+      iterations = it1;
       whole = tw, blocked = tb;
     }
-    if (!rc && blocked < whole * 0.98f) best_r = blk_r, best_chunk = blk_chunk, best_lanes = blk_lanes;
+    if (!rc && blocked < whole * 0.99f) best_r = blk_r, best_chunk = blk_chunk, best_lanes = blk_lanes;
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
