@@ -146,10 +146,13 @@ int spe_er(spe_engine* e, int first, int count, int iterations, float reality);
  * support (int32; NULL keeps the resident supports) go to slots
  * [first, first+count), run `iterations` of `algorithm` (SPE_OP_HIO / RAAR /
  * ER), and come back into density_out (may be `density`).  The population
- * is split into `blocks` blocks (<= 0: 2) on two streams, so one block's
- * copies overlap another's iterations; with page-locked host buffers the
- * copies are asynchronous.  Returns when density_out is complete.  Results
- * equal spe_upload + spe_hio/raar/er + spe_download. */
+ * is split into `blocks` blocks (<= 0: 2; more than count: count).  With
+ * two or more, uploads run in block order on one copy stream and downloads
+ * on another, and the blocks' iterations alternate between two streams
+ * (each kernel on half the GPU), so a block's copies overlap the other
+ * blocks' iterations; with page-locked host buffers the copies are
+ * asynchronous.  Returns when density_out is complete.  Results equal
+ * spe_upload + spe_hio/raar/er + spe_download. */
 int spe_iterate_host(spe_engine* e, int first, int count, const float* density, const int32_t* support,
                      int algorithm, int iterations, float beta, float reality, float* density_out, int blocks);
 

@@ -281,6 +281,18 @@ int ensure_lanes(spe_engine* e) {
   return SPE_OK;
 }
 
+// the copy streams of spe_iterate_host and at least `nev` block events
+int ensure_copy_streams(spe_engine* e, size_t nev) {
+  if (!e->h2d) CK(cudaStreamCreateWithFlags(&e->h2d, cudaStreamNonBlocking), "copy stream");
+  if (!e->d2h) CK(cudaStreamCreateWithFlags(&e->d2h, cudaStreamNonBlocking), "copy stream");
+  while (e->block_ev.size() < nev) {
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "block event");
+    e->block_ev.push_back(ev);
+  }
+  return SPE_OK;
+}
+
 // Runs `iters` iterations on [first, first+count) in blocks of `chunk`
 // individuals, each block through all its iterations before the next (the
 // individuals are independent, so the result equals one call on the whole
@@ -534,6 +546,12 @@ int spe_destroy(spe_engine* e) {
     cudaEventDestroy(e->join);
     cudaEventDestroy(e->phase);
   }
+  for (cudaStream_t s : {e->h2d, e->d2h})
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  for (cudaEvent_t ev : e->block_ev) cudaEventDestroy(ev);
   cudaStreamDestroy(e->own);
   delete e;
   return SPE_OK;
@@ -724,12 +742,15 @@ int spe_iterate_host(spe_engine* e, int first, int count, const float* density, 
   const int chunk = (count + blocks - 1) / blocks;
   const int nblocks = (count + chunk - 1) / chunk;
   const size_t np = e->npix;
-  CK(cudaEventRecord(e->fork, e->st), "fork");
-  CK(cudaStreamWaitEvent(e->lane2, e->fork, 0), "fork");
-  auto upload = [&](int b) -> int {
-    const int f = first + b * chunk, k = std::min(chunk, first + count - f);
-    const size_t h = (size_t)(f - first) * np;  // offset in the host arrays
-    cudaStream_t st = (b & 1) ? e->lane2 : e->st;
+  auto range = [&](int b, int* f, int* k, size_t* h) {
+    *f = first + b * chunk;
+    *k = std::min(chunk, first + count - *f);
+    *h = (size_t)(*f - first) * np;  // offset in the host arrays
+  };
+  auto upload = [&](int b, cudaStream_t st) -> int {
+    int f, k;
+    size_t h;
+    range(b, &f, &k, &h);
     CK(cudaMemcpyAsync(e->rho + (size_t)f * np, reinterpret_cast<const float2*>(density) + h,
                        (size_t)k * np * sizeof(float2), cudaMemcpyHostToDevice, st),
        "upload density");
@@ -739,34 +760,63 @@ int spe_iterate_host(spe_engine* e, int first, int count, const float* density, 
          "upload support");
     return SPE_OK;
   };
-  // With two blocks both uploads finish before either block iterates (they
-  // share the host link, so the first block would not start much earlier),
-  // and the second lane starts one column pass after the first, as in
-  // run_iterations: one block's row passes then run beside the other's
-  // column passes.  Left to the copies, the two lanes' relative phase is
-  // arbitrary, and lanes in phase measured 10% slower.
-  const bool paired = (nblocks == 2);
-  if (paired) {
-    if ((rc = upload(0)) || (rc = upload(1))) return rc;
-    CK(cudaEventRecord(e->join, e->lane2), "uploads");
-    CK(cudaStreamWaitEvent(e->st, e->join, 0), "uploads");
-  }
-  for (int b = 0; b < nblocks; ++b) {
-    const int f = first + b * chunk, k = std::min(chunk, first + count - f);
-    const size_t h = (size_t)(f - first) * np;  // offset in the host arrays
-    cudaStream_t st = (b & 1) ? e->lane2 : e->st;
-    if (!paired && (rc = upload(b))) return rc;
-    spe::Ctx c = make_ctx(e, f, k);
-    c.st = st;
-    c.grid_div = nblocks > 1 ? 2 : 1;
-    if (paired && b == 0) c.mark = e->phase;
-    if (paired && b == 1) CK(cudaStreamWaitEvent(e->lane2, e->phase, 0), "phase");
-    CK(e->ops->iterate(c, upd, iterations, beta, g, e->tile_cols, e->tile_rows), "iteration kernels");
+  auto download = [&](int b, cudaStream_t st) -> int {
+    int f, k;
+    size_t h;
+    range(b, &f, &k, &h);
     CK(cudaMemcpyAsync(reinterpret_cast<float2*>(density_out) + h, e->rho + (size_t)f * np,
                        (size_t)k * np * sizeof(float2), cudaMemcpyDeviceToHost, st),
        "download density");
+    return SPE_OK;
+  };
+  if (nblocks == 1) {
+    if ((rc = upload(0, e->st))) return rc;
+    CK(e->ops->iterate(make_ctx(e, first, count), upd, iterations, beta, g, e->tile_cols, e->tile_rows),
+       "iteration kernels");
+    if ((rc = download(0, e->st))) return rc;
+    CK(cudaStreamSynchronize(e->st), "synchronize");
+    return SPE_OK;
   }
-  CK(cudaEventRecord(e->join, e->lane2), "join");
+  // Blocks alternate between the engine's stream and the second lane, each
+  // kernel on half the resident CTAs.  Uploads run in block order on a copy
+  // stream and downloads on another, so block b's copies overlap the other
+  // blocks' iterations.  Both lanes start once the first two blocks are
+  // uploaded, the second one column pass after the first (as in
+  // run_iterations: one lane's row passes then run beside the other lane's
+  // column passes; lanes left in an arbitrary relative phase measured 10%
+  // slower), and equal blocks keep that offset.  The downloads are queued
+  // after every iteration, so a download into pageable memory, which holds
+  // the host thread until it completes, delays no launch.
+  if ((rc = ensure_copy_streams(e, 2 * (size_t)nblocks))) return rc;
+  cudaEvent_t* uploaded = e->block_ev.data();
+  cudaEvent_t* iterated = uploaded + nblocks;
+  CK(cudaEventRecord(e->fork, e->st), "fork");
+  for (cudaStream_t s : {e->lane2, e->h2d, e->d2h}) CK(cudaStreamWaitEvent(s, e->fork, 0), "fork");
+  for (int b = 0; b < nblocks; ++b) {
+    if ((rc = upload(b, e->h2d))) return rc;
+    CK(cudaEventRecord(uploaded[b], e->h2d), "upload event");
+  }
+  for (int b = 0; b < nblocks; ++b) {
+    int f, k;
+    size_t h;
+    range(b, &f, &k, &h);
+    cudaStream_t st = (b & 1) ? e->lane2 : e->st;
+    CK(cudaStreamWaitEvent(st, uploaded[b == 0 ? 1 : b], 0), "upload wait");
+    spe::Ctx c = make_ctx(e, f, k);
+    c.st = st;
+    c.grid_div = 2;
+    if (b == 0) c.mark = e->phase;
+    if (b == 1) CK(cudaStreamWaitEvent(e->lane2, e->phase, 0), "phase");
+    CK(e->ops->iterate(c, upd, iterations, beta, g, e->tile_cols, e->tile_rows), "iteration kernels");
+    CK(cudaEventRecord(iterated[b], st), "iteration event");
+  }
+  for (int b = 0; b < nblocks; ++b) {
+    CK(cudaStreamWaitEvent(e->d2h, iterated[b], 0), "iteration wait");
+    if ((rc = download(b, e->d2h))) return rc;
+  }
+  // the last download follows every block's iteration, and each iteration
+  // its upload: joining the download stream joins all four
+  CK(cudaEventRecord(e->join, e->d2h), "join");
   CK(cudaStreamWaitEvent(e->st, e->join, 0), "join");
   CK(cudaStreamSynchronize(e->st), "synchronize");
   return SPE_OK;

@@ -51,6 +51,10 @@ struct spe_engine {
   int* dev_err = nullptr;  // device flag of the kernels' bounded waits
   cudaStream_t lane2 = nullptr;          // second lane (created on first use)
   cudaEvent_t fork = nullptr, join = nullptr, phase = nullptr;
+  // copy streams of spe_iterate_host and its per-block events (uploaded,
+  // iterated), grown on demand
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  std::vector<cudaEvent_t> block_ev;
 };
 
 

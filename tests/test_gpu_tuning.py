@@ -127,7 +127,7 @@ def test_autotune_schedule_is_valid():
     assert np.array_equal(got, dens)
 
 
-@pytest.mark.parametrize("blocks", [0, 1, 3, 7])
+@pytest.mark.parametrize("blocks", [0, 1, 2, 3, 4, 7])
 def test_iterate_host_equals_upload_iterate_download(blocks):
     """The pipelined host-buffer call gives the same results as separate
     upload, iteration and download calls."""
@@ -142,3 +142,31 @@ def test_iterate_host_equals_upload_iterate_download(blocks):
     buf = dens.copy()
     e.iterate_host(0, buf, None, _lib.SPE_OP_RAAR, 5, 0.87, 0.0, out=buf, blocks=blocks)
     assert np.array_equal(buf.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("alg,blocks", [(_lib.SPE_OP_HIO, 4), (_lib.SPE_OP_ER, 5), (_lib.SPE_OP_RAAR, 8)])
+def test_iterate_host_pinned_in_place(alg, blocks):
+    """Page-locked host buffers (asynchronous copies on the call's copy
+    streams), results written over the input: equal to separate upload,
+    iteration and download calls, slots outside the range untouched."""
+    import torch
+
+    n, P = 256, 16
+    e, dens, S = engine(n, P, seed=11)
+    e.upload(0, dens, S)
+    {_lib.SPE_OP_HIO: lambda: e.hio(0, P - 2, 7, 0.9, 0.0), _lib.SPE_OP_ER: lambda: e.er(0, P - 2, 7, 0.0),
+     _lib.SPE_OP_RAAR: lambda: e.raar(0, P - 2, 7, 0.87, 0.0)}[alg]()
+    ref, _ = e.download(0, P)
+    e.upload(0, dens, S)
+    h = torch.empty((P - 2, n, n, 2), dtype=torch.float32, pin_memory=True)
+    hs = torch.empty((P - 2, n, n), dtype=torch.int32, pin_memory=True)
+    h.numpy()[...] = dens[: P - 2].view(np.float32).reshape(P - 2, n, n, 2)
+    hs.numpy()[...] = S[: P - 2]
+    fp = lambda t: _lib.C.cast(t.data_ptr(), _lib.C.POINTER(_lib.C.c_float))
+    ip = lambda t: _lib.C.cast(t.data_ptr(), _lib.C.POINTER(_lib.C.c_int32))
+    beta = {_lib.SPE_OP_HIO: 0.9, _lib.SPE_OP_ER: 0.0, _lib.SPE_OP_RAAR: 0.87}[alg]
+    _lib.call("spe_iterate_host", e.h, 0, P - 2, fp(h), ip(hs), alg, 7, beta, 0.0, fp(h), blocks)
+    got = h.numpy().reshape(P - 2, n, n, 2).view(np.complex64).reshape(P - 2, n, n)
+    assert np.array_equal(got.view(np.uint32), ref[: P - 2].view(np.uint32))
+    rest, _ = e.download(P - 2, 2)
+    assert np.array_equal(rest.view(np.uint32), dens[P - 2:].view(np.uint32))
