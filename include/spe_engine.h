@@ -265,12 +265,14 @@ int spe_crossover_draws(uint32_t seed, int count, const int32_t* order, float su
 
 /* Tile widths of the iteration kernels: columns per column-pass tile and
  * rows per row-pass tile (0: the built-in defaults).  Column codes: W (the
- * swizzled exchange layout), -W (two columns per thread), 100+W (one warp per
- * column), 200+W (one barrier group per column), 300+W (padded exchange
- * layout).  Row codes: W (exchange padding l + l/16), 100+W (padding chosen
- * per exchange).  Every code computes bit-identical results; only codes
- * compiled for the engine's pattern size are accepted (spe_autotune times
- * them all). */
+ * swizzled exchange layout), -W (two columns per thread), 100+W (one warp
+ * per column), 200+W (one barrier group per column), 300+W (padded
+ * exchange layout), 600+W (two columns per thread in packed registers).
+ * Row codes: W (exchange padding l + l/16), 100+W (padding chosen per
+ * exchange), 400+W (two rows per thread in packed registers), 500+W /
+ * 600+W (tiles moved by TMA, either padding), 700+W (one stage instead of
+ * two).  Every code computes bit-identical results; only codes compiled for
+ * the engine's pattern size are accepted (spe_autotune times them all). */
 int spe_set_tiles(spe_engine* e, int cols, int rows);
 int spe_get_tiles(spe_engine* e, int* cols, int* rows);
 
